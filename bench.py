@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""BC1 encoder benchmark: Gpixel/s per quality level on the quality-sweep workload.
+
+Workload (one "step"): the 4096x4096 RGBA8 quality-sweep image (seeded
+gradients + 4-octave value noise + rectangles, 5% single-colour and 5%
+near-black blocks, alpha from a second noise field) encoded at every quality
+level 0..9 with color_weights {0.299, 0.587, 0.114}, input_weights =
+alpha / 255, D3D10, three_color_mode = three_color_black = true.  The
+headline value is the whole sweep's throughput: 10 x 16.8 Mpx / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU implementation of the same path (the C
+restatement of the reference's scalar encoder, every host thread) on a bounded
+sample of the same workload.  Under torchrun each rank encodes its own replica
+(the path has no exchange step); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BC1 Gpixel/s per quality level, batched vs plain, bit-exact; serving p50/p99 ms"
+UNIT = "Gpixel/s"
+CW = (0.299, 0.587, 0.114)
+LEVELS = list(range(10))
+
+# Algorithmic FP32 operations per unit of work, counted from the reference's
+# scalar encoder (icbc.h v1.05): one op per float add/sub/mul/div/compare/
+# min/max/abs/convert executed by the ICBC_SIMD=0 build.
+OPS_PER_UNIT = {
+    "cf4_combos": 140,     # cluster_fit_four iteration, icbc.h:2650-2733
+    "cf3_combos": 123,     # cluster_fit_three iteration, icbc.h:2273-2335
+    "refine_steps": 996,   # refine_endpoints step: palette, compute_indices, evaluate_mse, icbc.h:3614-3648
+    "out4_blocks": 950,    # output_block4: 565 quantise, palette, compute_indices4, evaluate_mse
+    "out3_blocks": 915,    # output_block3
+    "single_blocks": 283,  # single-colour path + evaluate_mse, icbc.h:3761-3764
+    "sat_builds": 151,     # compute_sat fixed part: power iterations, normalisation
+    "sat_points": 37,      # compute_sat per colour: centroid, covariance, projection, prefix sums
+    "reduce_pairs": 9,     # reduce_colors equal() test
+    "reduce_merges": 13,   # reduce_colors weighted merge
+    "box_fits": 41,        # inset_bbox + select_diagonal fixed part
+    "box_points": 13,      # fit_colors_bbox + select_diagonal per colour
+    "lsq_fits": 378,       # optimize_end_points4
+}
+REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
+
+
+def algorithmic_ops(stats: dict, level: int) -> float:
+    ops = sum(OPS_PER_UNIT[k] * stats.get(k, 0) for k in OPS_PER_UNIT)
+    if level >= 2:
+        ops += REDUCE_PER_BLOCK * stats["blocks"]
+    return float(ops)
+
+
+def load_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        p["source"] = "measured"
+        return p
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+def fp32_peak_tops(peaks: dict, sms: int) -> float:
+    """Non-FMA FP32 peak: 128 lanes per SM x SMs x max SM clock (ops/s / 1e12)."""
+    return 128 * sms * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+            time.sleep(0.5)
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def mark(self, begin: bool):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.2)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        inside = [r for t, r in self.rows if self.t0 and self.t1 and self.t0 <= t <= self.t1 + 0.05]
+        if not inside:
+            inside = [r for _, r in self.rows]
+        sm = [float(r[1]) for r in inside if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in inside if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in inside:
+            if len(r) > 8:
+                for name, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(inside)}
+
+
+def sample_rows(img: np.ndarray, stride: int) -> np.ndarray:
+    """Every stride-th row of 4x4 blocks (whole blocks, same width)."""
+    h = img.shape[0]
+    rows = [img[y:y + 4] for y in range(0, h - h % 4, 4 * stride)]
+    return np.ascontiguousarray(np.concatenate(rows, axis=0))
+
+
+def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=LEVELS):
+    """Times the oracle (CPU restatement of the reference encoder) on the sample."""
+    from oracle import oracle as O
+    O.lib()  # build/load outside the timed region
+    times, stats, outs = {}, {}, {}
+    for lv in levels:
+        t0 = time.perf_counter()
+        b, _, st = O.encode_image(img_sample, lv, 0, CW, 1, None, True, True, nthreads=nthreads, with_stats=True)
+        times[lv] = time.perf_counter() - t0
+        stats[lv] = st
+        outs[lv] = b
+    return times, stats, outs
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from icbc_gb300 import synth
+    img = synth.quality_sweep_image(args.size, args.size, seed=1)
+    sample = sample_rows(img, args.cpu_stride)
+    px = sample.shape[0] * sample.shape[1]
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sweep(sample, nthreads, levels=[0])
+    step_times = []
+    per_level = {lv: [] for lv in LEVELS}
+    for _ in range(args.steps):
+        times, _, _ = cpu_sweep(sample, nthreads)
+        step_times.append(sum(times.values()))
+        for lv in LEVELS:
+            per_level[lv].append(times[lv])
+    t = statistics.mean(step_times)
+    value = len(LEVELS) * px / t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "quality_sweep_%dx%d_L0-9" % (args.size, args.size), "levels": LEVELS,
+                   "color_weights": CW, "input_weights": "alpha/255", "decoder": "D3D10",
+                   "three_color_mode": True, "three_color_black": True,
+                   "sample": "every %dth row of 4x4 blocks (%d px per level)" % (args.cpu_stride, px)},
+        "per_level": {str(lv): len(per_level[lv]) and px / statistics.mean(per_level[lv]) / 1e9 for lv in LEVELS},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "every %dth block row of the workload, all 10 levels" % args.cpu_stride},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import icbc_gb300 as ig
+    from icbc_gb300 import synth
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    ig.init(ig.Decoder_D3D10)
+    sms = ig.load().icbc_gpu_sm_count()
+
+    img = synth.quality_sweep_image(args.size, args.size, seed=1)
+    h, w = img.shape[:2]
+    px = h * w
+    nb = ig.blocks_of(w, h)
+    d_img = torch.from_numpy(img).to(dev)
+    outs = {lv: torch.zeros((nb, 8), dtype=torch.uint8, device=dev) for lv in LEVELS}
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def encode(lv):
+        ig.compress_image(d_img, lv, ig.Decoder_D3D10, CW, weight_mode=ig.WEIGHTS_ALPHA, out=outs[lv], stream=stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            for lv in LEVELS:
+                encode(lv)
+    torch.cuda.synchronize()
+
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in LEVELS]
+          for _ in range(args.steps)]
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.mark(True)
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush (256 MB written) between steps, outside the timed events
+            for i, lv in enumerate(LEVELS):
+                ev[k][i][0].record(stream)
+                encode(lv)
+                ev[k][i][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clocks.mark(False)
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    lvl_ms = {lv: statistics.mean(ev[k][i][0].elapsed_time(ev[k][i][1]) for k in range(args.steps))
+              for i, lv in enumerate(LEVELS)}
+    step_ms = sum(lvl_ms.values())
+    if ws > 1:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = ws * len(LEVELS) * px / (step_ms * 1e-3) / 1e9
+
+    # End to end through the host-buffer C-ABI call: pinned image in, blocks out.
+    pin = torch.from_numpy(img).pin_memory()
+    host_img = pin.numpy()
+    host_out = {lv: torch.zeros((nb, 8), dtype=torch.uint8).pin_memory().numpy() for lv in LEVELS}
+    for lv in LEVELS:
+        ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
+    e2e_steps = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for lv in LEVELS:
+            ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
+    e2e_t = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = ws * len(LEVELS) * px / e2e_t / 1e9
+    h2d = len(LEVELS) * img.nbytes + sum(nb * 8 for lv in LEVELS if lv >= 4)
+    d2h = len(LEVELS) * nb * 8
+
+    if rank != 0:
+        return
+    # CPU baseline + algorithmic op counts + sampled parity on every level.
+    sample = sample_rows(img, args.cpu_stride)
+    sample_px = sample.shape[0] * sample.shape[1]
+    nthreads = os.cpu_count() or 1
+    ctimes, cstats, couts = cpu_sweep(sample, nthreads)
+    cpu_value = len(LEVELS) * sample_px / sum(ctimes.values()) / 1e9
+    bw = w // 4
+    rows = list(range(0, h // 4, args.cpu_stride))
+    mismatches = {}
+    for lv in LEVELS:
+        gpu = outs[lv].cpu().numpy().reshape(h // 4, bw, 8)[rows].reshape(-1, 8)
+        mismatches[str(lv)] = int((gpu != couts[lv]).any(1).sum())
+    scale = nb / sum(s["blocks"] for s in [cstats[0]])
+    ops = {lv: algorithmic_ops(cstats[lv], lv) * scale for lv in LEVELS}
+    peaks = load_peaks()
+    peak = fp32_peak_tops(peaks, sms)
+    top = max(LEVELS, key=lambda lv: lvl_ms[lv])
+    achieved = ops[top] / (lvl_ms[top] * 1e-3) / 1e12
+    per_level = {str(lv): {"gpix_s": px / (lvl_ms[lv] * 1e-3) / 1e9, "ms": lvl_ms[lv],
+                           "fp32_frac": ops[lv] / (lvl_ms[lv] * 1e-3) / 1e12 / peak,
+                           "cpu_gpix_s": sample_px / ctimes[lv] / 1e9} for lv in LEVELS}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    l0_bytes = px * 4 + nb * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "quality_sweep_%dx%d_L0-9" % (w, h), "levels": LEVELS, "color_weights": CW,
+                   "input_weights": "alpha/255", "decoder": "D3D10", "three_color_mode": True,
+                   "three_color_black": True, "form": "plain (one launch per level)",
+                   "l2": "flushed between steps (256 MB write outside the timed events)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "per_level": per_level,
+        "mismatches_sampled": mismatches,
+        "roofline": {"bound": "fp32", "kernel": "k_encode_image<%d>" % top, "achieved": achieved, "peak": peak,
+                     "unit": "Tops/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "128 FP32 lanes x %d SMs x %s MHz (%s sm_max_mhz)" % (
+                         sms, peaks.get("sm_max_mhz"), peaks["source"])},
+        "roofline_hbm_level0": {"bound": "hbm", "achieved": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9, "peak": hbm,
+                                "unit": "GB/s", "frac": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9 / hbm,
+                                "traffic": None},
+        "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "every %dth block row (%d px) at all 10 levels" % (args.cpu_stride, sample_px)},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step"},
+        "gpu_launches": args.steps * len(LEVELS),
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--cpu-stride", type=int, default=8)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,342 @@
+"""icbc_gb300 -- GB300 (sm_103a) BC1 encoder, a drop-in for icbc's compress path.
+
+Python mirror of the icbc.h surface (``init``, ``compress_bc1``,
+``decode_bc1``, ``evaluate_bc1_error`` with the same enum values and argument
+meanings) plus the batched forms, all calling the CUDA kernels through the C
+ABI of ``include/icbc_gpu.h`` (``icbc_gb300/_lib/libicbc_gpu.so``).  There is
+no CPU fallback: without the built library and a CUDA device every call
+raises.  PyTorch is used only to hold device buffers and streams.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+from . import _build
+
+# icbc::Decoder (icbc.h:12-17)
+Decoder_D3D10, Decoder_NVIDIA, Decoder_AMD, Decoder_Intel = 0, 1, 2, 3
+DECODER_DEFAULT = -1
+# icbc::Quality (icbc.h:21-36)
+(Quality_Level0, Quality_Level1, Quality_Level2, Quality_Level3, Quality_Level4, Quality_Level5,
+ Quality_Level6, Quality_Level7, Quality_Level8, Quality_Level9) = range(10)
+Quality_Fast, Quality_Default, Quality_Max = 1, 8, 9
+# weight sources of RGBA8 images
+WEIGHTS_UNIFORM, WEIGHTS_ALPHA, WEIGHTS_PLANE = 0, 1, 2
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "not initialized", 3: "CUDA error", 4: "out of memory",
+          5: "misaligned", 6: "over budget", 7: "not ready", 8: "cancelled", 9: "not found"}
+
+
+class IcbcGpuError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        super().__init__("%s failed: %s%s" % (what, STATUS.get(status, status), (" (%s)" % detail) if detail else ""))
+
+
+class ImageDesc(ctypes.Structure):
+    """struct icbc_gpu_image (include/icbc_gpu.h)."""
+    _fields_ = [("rgba", ctypes.c_void_p), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("pitch", ctypes.c_int64), ("weight_mode", ctypes.c_int32), ("weight_plane", ctypes.c_void_p),
+                ("weight_pitch", ctypes.c_int64), ("level", ctypes.c_int32), ("decoder", ctypes.c_int32),
+                ("three_color_mode", ctypes.c_int32), ("three_color_black", ctypes.c_int32),
+                ("color_weights", ctypes.c_float * 3), ("out", ctypes.c_void_p), ("errors", ctypes.c_void_p)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Loads libicbc_gpu.so (building it first if asked).  Raises if absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError("icbc_gb300: %s is missing; run icbc_gb300._build.build()" % path)
+        L = ctypes.CDLL(path)
+        i32, i64, vp, f32p = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)
+        sig = {
+            "icbc_gpu_init": (i32, [i32]),
+            "icbc_gpu_get_decoder": (i32, []),
+            "icbc_gpu_status_string": (ctypes.c_char_p, [i32]),
+            "icbc_gpu_last_error": (ctypes.c_char_p, []),
+            "icbc_gpu_sm_count": (i32, []),
+            "icbc_gpu_compress_bc1_blocks": (i32, [i32, vp, vp, f32p, i32, i32, i32, vp, vp, i64, vp]),
+            "icbc_gpu_compress_bc1_image": (i32, [ctypes.POINTER(ImageDesc), vp]),
+            "icbc_gpu_batch_create": (i32, [ctypes.POINTER(ImageDesc), i32, ctypes.POINTER(vp)]),
+            "icbc_gpu_batch_launch": (i32, [vp, vp]),
+            "icbc_gpu_batch_destroy": (i32, [vp]),
+            "icbc_gpu_compress_bc1_images": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
+            "icbc_gpu_decode_bc1": (i32, [vp, vp, i64, i32, vp]),
+            "icbc_gpu_evaluate_bc1_error": (i32, [vp, vp, vp, i64, i32, vp]),
+            "icbc_gpu_compress_bc1_image_host": (i32, [vp, i32, i32, i64, i32, vp, i32, i32, i32, i32, f32p, vp, vp]),
+            "icbc_gpu_debug_tables": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        detail = ""
+        if status == 3 and _lib is not None:
+            detail = (_lib.icbc_gpu_last_error() or b"").decode()
+        raise IcbcGpuError(status, what, detail)
+
+
+def _cw(color_weights):
+    arr = (ctypes.c_float * 3)(*[float(x) for x in color_weights])
+    return arr
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("icbc_gb300 needs a CUDA device (no CPU fallback)")
+    return torch
+
+
+def _stream_ptr(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+# ------------------------------------------------------------ icbc.h mirror
+
+def init(decoder: int = Decoder_D3D10) -> None:
+    """icbc::init (icbc.h:19): uploads the tables and sets the default decoder."""
+    _check(load().icbc_gpu_init(int(decoder)), "init")
+
+
+def get_decoder() -> int:
+    return load().icbc_gpu_get_decoder()
+
+
+def compress_bc1(level: int, input_colors, input_weights, color_weights, three_color_mode: bool,
+                 three_color_black: bool, output=None) -> float:
+    """icbc::compress_bc1 (icbc.h:48) for one block: 16x4 floats in, 8 bytes out.
+
+    Returns the block's weighted error; writes the block into ``output``
+    (a writable 8-byte buffer) when given and returns (error, bytes) otherwise.
+    One synchronous device round trip: a correctness path, not a fast one.
+    """
+    cols = np.ascontiguousarray(input_colors, np.float32).reshape(1, 16, 4)
+    w = np.ascontiguousarray(input_weights, np.float32).reshape(1, 16)
+    prev = None
+    if output is not None:
+        prev = np.frombuffer(output, dtype=np.uint8, count=8).reshape(1, 8).copy()
+    blocks, errors = compress_blocks(cols, w, level, color_weights=color_weights,
+                                     three_color_mode=three_color_mode, three_color_black=three_color_black,
+                                     decoder=DECODER_DEFAULT, initial=prev)
+    blocks = blocks.cpu().numpy() if hasattr(blocks, "cpu") else blocks
+    errors = errors.cpu().numpy() if hasattr(errors, "cpu") else errors
+    if output is not None:
+        np.frombuffer(output, dtype=np.uint8, count=8)[:] = blocks[0]
+        return float(errors[0])
+    return float(errors[0]), bytes(blocks[0])
+
+
+def decode_bc1(block, decoder: int = Decoder_D3D10) -> np.ndarray:
+    """icbc::decode_bc1 (icbc.h:38) for one block -> 64 RGBA8 bytes."""
+    torch = _torch()
+    b = torch.as_tensor(np.frombuffer(bytes(block), np.uint8).reshape(1, 8)).cuda()
+    return decode_blocks(b, decoder).cpu().numpy().reshape(64)
+
+
+def evaluate_bc1_error(rgba_block, block, decoder: int = Decoder_D3D10) -> float:
+    """icbc::evaluate_bc1_error (icbc.h:43) for one block."""
+    torch = _torch()
+    t = torch.as_tensor(np.ascontiguousarray(rgba_block, np.uint8).reshape(1, 64)).cuda()
+    b = torch.as_tensor(np.frombuffer(bytes(block), np.uint8).reshape(1, 8)).cuda()
+    return float(evaluate_errors(t, b, decoder).cpu()[0])
+
+
+def debug_tables(decoder: int) -> dict:
+    """The init-time tables the library builds (host only, no GPU needed)."""
+    L = load()
+    t = {"match5": np.zeros(512, np.uint8), "match6": np.zeros(512, np.uint8), "weights": np.zeros(5, np.float32),
+         "four": np.zeros(968, np.uint32), "four_total": np.zeros(16, np.int32), "three": np.zeros(152, np.uint32),
+         "three_total": np.zeros(16, np.int32)}
+    _check(L.icbc_gpu_debug_tables(int(decoder), *[t[k].ctypes.data for k in
+                                                   ("match5", "match6", "weights", "four", "four_total", "three",
+                                                    "three_total")]), "debug_tables")
+    return t
+
+
+# ---------------------------------------------------------- batched forms
+
+def compress_blocks(colors, weights, level: int, decoder: int = DECODER_DEFAULT, color_weights=(1.0, 1.0, 1.0),
+                    three_color_mode: bool = True, three_color_black: bool = True, initial=None, stream=None,
+                    out=None, errors=None):
+    """Encodes n blocks given as compress_bc1 inputs.
+
+    colors: (n,16,4) float32, weights: (n,16) float32 or None (1.0f).  numpy
+    arrays are copied to the device and results come back as numpy; CUDA
+    tensors stay on the device and (blocks uint8 (n,8), errors float32 (n,))
+    tensors are returned.  ``initial`` seeds the output bytes (kept by levels
+    4..9 when no candidate has a finite error, as the reference does).
+    """
+    torch = _torch()
+    L = load()
+    on_host = not (hasattr(colors, "is_cuda") and colors.is_cuda)
+    dev = torch.device("cuda")
+    c = torch.as_tensor(np.ascontiguousarray(colors, np.float32) if on_host else colors).to(dev)
+    c = c.reshape(-1, 64).contiguous()
+    n = c.shape[0]
+    w = None
+    if weights is not None:
+        w = torch.as_tensor(np.ascontiguousarray(weights, np.float32) if on_host else weights).to(dev)
+        w = w.reshape(n, 16).contiguous()
+    if out is None:
+        out = torch.zeros((n, 8), dtype=torch.uint8, device=dev)
+        if initial is not None:
+            out.copy_(torch.as_tensor(np.ascontiguousarray(initial, np.uint8)).reshape(n, 8))
+    if errors is None:
+        errors = torch.empty(n, dtype=torch.float32, device=dev)
+    cw = _cw(color_weights)
+    st = L.icbc_gpu_compress_bc1_blocks(int(level), c.data_ptr(), None if w is None else w.data_ptr(), cw,
+                                        int(bool(three_color_mode)), int(bool(three_color_black)), int(decoder),
+                                        out.data_ptr(), errors.data_ptr(), n, _stream_ptr(stream))
+    _check(st, "compress_bc1_blocks")
+    if on_host:
+        torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
+        return out.cpu().numpy(), errors.cpu().numpy()
+    return out, errors
+
+
+def image_desc(rgba, level: int, out, errors=None, decoder: int = DECODER_DEFAULT, color_weights=(1.0, 1.0, 1.0),
+               weight_mode: int = WEIGHTS_UNIFORM, weight_plane=None, three_color_mode: bool = True,
+               three_color_black: bool = True, width: int | None = None, height: int | None = None,
+               pitch: int | None = None) -> ImageDesc:
+    """Builds an icbc_gpu_image for a CUDA uint8 tensor of shape (h, w, 4)
+    (or a flat buffer with explicit width/height/pitch)."""
+    d = ImageDesc()
+    if width is None:
+        height, width = int(rgba.shape[0]), int(rgba.shape[1])
+        pitch = int(rgba.stride(0))
+    d.rgba = rgba.data_ptr()
+    d.width, d.height, d.pitch = int(width), int(height), int(pitch)
+    d.weight_mode = int(weight_mode)
+    d.weight_plane = weight_plane.data_ptr() if weight_plane is not None else None
+    d.weight_pitch = int(weight_plane.stride(0)) if weight_plane is not None else 0
+    d.level, d.decoder = int(level), int(decoder)
+    d.three_color_mode, d.three_color_black = int(bool(three_color_mode)), int(bool(three_color_black))
+    d.color_weights = (ctypes.c_float * 3)(*[float(x) for x in color_weights])
+    d.out = out.data_ptr()
+    d.errors = errors.data_ptr() if errors is not None else None
+    return d
+
+
+def blocks_of(width: int, height: int) -> int:
+    return ((width + 3) // 4) * ((height + 3) // 4)
+
+
+def compress_image(rgba, level: int, decoder: int = DECODER_DEFAULT, color_weights=(1.0, 1.0, 1.0),
+                   weight_mode: int = WEIGHTS_UNIFORM, weight_plane=None, three_color_mode: bool = True,
+                   three_color_black: bool = True, out=None, errors=None, with_errors: bool = False, stream=None):
+    """Plain form: one launch for one RGBA8 image (CUDA uint8 tensor (h,w,4))."""
+    torch = _torch()
+    L = load()
+    h, w = int(rgba.shape[0]), int(rgba.shape[1])
+    nb = blocks_of(w, h)
+    if out is None:
+        out = torch.zeros((nb, 8), dtype=torch.uint8, device=rgba.device)
+    if errors is None and with_errors:
+        errors = torch.empty(nb, dtype=torch.float32, device=rgba.device)
+    d = image_desc(rgba, level, out, errors, decoder, color_weights, weight_mode, weight_plane, three_color_mode,
+                   three_color_black)
+    _check(L.icbc_gpu_compress_bc1_image(ctypes.byref(d), _stream_ptr(stream)), "compress_bc1_image")
+    return (out, errors) if with_errors else out
+
+
+class Batch:
+    """A planned batched launch over many images (icbc_gpu_batch_*)."""
+
+    def __init__(self, descs: Sequence[ImageDesc], keepalive=()):
+        L = load()
+        arr = (ImageDesc * len(descs))(*descs)
+        h = ctypes.c_void_p()
+        _check(L.icbc_gpu_batch_create(arr, len(descs), ctypes.byref(h)), "batch_create")
+        self._h = h
+        self._keep = list(keepalive)
+
+    def launch(self, stream=None):
+        _check(load().icbc_gpu_batch_launch(self._h, _stream_ptr(stream)), "batch_launch")
+
+    def close(self):
+        if self._h:
+            load().icbc_gpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def decode_blocks(blocks, decoder: int = Decoder_D3D10, stream=None):
+    """decode_bc1 over a CUDA uint8 tensor (n,8) -> (n,64) RGBA8."""
+    torch = _torch()
+    n = blocks.shape[0]
+    out = torch.empty((n, 64), dtype=torch.uint8, device=blocks.device)
+    _check(load().icbc_gpu_decode_bc1(blocks.contiguous().data_ptr(), out.data_ptr(), n, int(decoder),
+                                      _stream_ptr(stream)), "decode_bc1")
+    return out
+
+
+def evaluate_errors(rgba_blocks, blocks, decoder: int = Decoder_D3D10, stream=None):
+    """evaluate_bc1_error over CUDA tensors (n,64) uint8 and (n,8) uint8 -> (n,) float32."""
+    torch = _torch()
+    n = blocks.shape[0]
+    out = torch.empty(n, dtype=torch.float32, device=blocks.device)
+    _check(load().icbc_gpu_evaluate_bc1_error(rgba_blocks.contiguous().data_ptr(), blocks.contiguous().data_ptr(),
+                                              out.data_ptr(), n, int(decoder), _stream_ptr(stream)),
+           "evaluate_bc1_error")
+    return out
+
+
+def compress_image_host(rgba: np.ndarray, level: int, decoder: int = DECODER_DEFAULT,
+                        color_weights=(1.0, 1.0, 1.0), weight_mode: int = WEIGHTS_UNIFORM, weight_plane=None,
+                        three_color_mode: bool = True, three_color_black: bool = True, out=None, errors=None):
+    """End-to-end call on host buffers: H2D, encode, D2H (synchronous).
+    rgba: (h,w,4) uint8 (pinned memory gives the fastest copies)."""
+    L = load()
+    h, w = int(rgba.shape[0]), int(rgba.shape[1])
+    nb = blocks_of(w, h)
+    if out is None:
+        out = np.zeros((nb, 8), np.uint8)
+    plane_ptr = None
+    if weight_mode == WEIGHTS_PLANE:
+        weight_plane = np.ascontiguousarray(weight_plane, np.float32)
+        plane_ptr = weight_plane.ctypes.data
+    pitch = rgba.strides[0] if isinstance(rgba, np.ndarray) else 4 * w
+    ptr = rgba.ctypes.data if isinstance(rgba, np.ndarray) else rgba.data_ptr()
+    optr = out.ctypes.data if isinstance(out, np.ndarray) else out.data_ptr()
+    eptr = None
+    if errors is not None:
+        eptr = errors.ctypes.data if isinstance(errors, np.ndarray) else errors.data_ptr()
+    st = L.icbc_gpu_compress_bc1_image_host(ptr, w, h, pitch, int(weight_mode), plane_ptr, int(level), int(decoder),
+                                            int(bool(three_color_mode)), int(bool(three_color_black)),
+                                            _cw(color_weights), optr, eptr)
+    _check(st, "compress_bc1_image_host")
+    return out

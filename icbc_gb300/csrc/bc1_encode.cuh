@@ -1,0 +1,563 @@
+// bc1_encode.cuh -- the BC1 block encoder for one warp of 32 blocks.
+//
+// Work split inside a warp:
+//   * serial stages of icbc's compress_bc1 (reduce_colors, box fit, least
+//     squares, PCA + summed-area table, index selection, refinement) run one
+//     block per lane;
+//   * the 4- and 3-cluster enumerations (the hot loops) run cooperatively:
+//     the 32 lanes split one block's table of boundary combinations, keep the
+//     first strict minimum of their share and reduce with warp shuffles,
+//     ties going to the lowest table index -- the same winner the sequential
+//     loop of icbc.h:2362-2733 keeps.
+//
+// Shared memory per warp, [32 blocks][odd stride] so that per-lane rows are
+// conflict-free and one block's SAT can be read by all lanes at once:
+//   in    [32][65]  texels r,g,b (float) + weight, 16 x 4 floats
+//   red   [32][65]  reduced colours + weights (reduce_colors / skip_blacks)
+//   sat   [32][69]  SAT with a leading zero: comp c at [c*17 + 0..16]
+#pragma once
+
+#include "bc1_device.cuh"
+
+namespace icbc_gpu {
+
+constexpr int kWarpsPerCta = 4;
+constexpr int kInStride = 65;
+constexpr int kSatStride = 69;
+constexpr unsigned kFull = 0xffffffffu;
+
+constexpr size_t kWarpFloatsLow = 32 * kInStride;                                  // L0, L1
+constexpr size_t kWarpFloatsHigh = 32 * kInStride * 2 + 32 * kSatStride;          // L2..L9
+
+__host__ __device__ constexpr size_t smem_bytes(bool cluster_fit) {
+    return sizeof(SharedTables) + kWarpsPerCta * 4 * (cluster_fit ? kWarpFloatsHigh : kWarpFloatsLow);
+}
+
+// Options of each quality level (setup_options, icbc.h:3663-3731).
+template <int L>
+struct Level {
+    static constexpr bool box = L <= 3;
+    static constexpr bool lsq = L == 1 || L == 2;
+    static constexpr bool cluster = L >= 2;
+    static constexpr bool cf3_black_only = L >= 2 && L <= 7;
+    static constexpr bool cf3_always = L >= 8;
+    static constexpr bool refine = L == 9;
+    static constexpr float threshold = L == 2 ? 1.0f / 24 : L == 3 ? 1.0f / 32 : L == 4 ? 1.0f / 48
+                                     : L == 5 ? 1.0f / 64 : L == 6 ? 1.0f / 96 : L == 7 ? 1.0f / 128
+                                     : L >= 8 ? 1.0f / 256 : 0.0f;
+};
+
+// Refinement step deltas (icbc.h:3584-3609).
+__constant__ int8_t c_deltas[16][3] = {
+    {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1},
+    {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {-1, -1, 0}, {-1, 0, -1}, {0, -1, -1},
+    {-1, 1, 0}, {1, -1, 0}, {0, -1, 1}, {0, 1, -1}};
+
+struct EncodeParams {
+    int decoder;
+    int three_color_mode;
+    int three_color_black;
+    V3 cw;
+};
+
+// Everything one warp needs for a group of 32 blocks.
+struct WarpCtx {
+    const SharedTables *T;
+    const DecoderTables *D;
+    float *in;
+    float *red;
+    float *sat;
+    int lane;
+};
+
+// ------------------------------------------------------------ per lane --
+
+// reduce_colors (icbc.h:1683-1728) into this lane's `red` row.
+__device__ __forceinline__ int reduce_colors(const float *row, float threshold, float *rrow, bool &any_black) {
+    int n = 0;
+    any_black = false;
+    for (int i = 0; i < 16; i++) {
+        const V3 ci = texel(row, i);
+        const float wi = row[4 * i + 3];
+        if (wi > 0) {
+            int j = 0;
+            for (; j < n; j++) {
+                const V3 cj = texel(rrow, j);
+                if (near3(cj, ci, threshold)) {
+                    const float wj = rrow[4 * j + 3];
+                    const float s = wj + wi;
+                    rrow[4 * j + 0] = (cj.x * wj + ci.x * wi) / s;
+                    rrow[4 * j + 1] = (cj.y * wj + ci.y * wi) / s;
+                    rrow[4 * j + 2] = (cj.z * wj + ci.z * wi) / s;
+                    rrow[4 * j + 3] = s;
+                    break;
+                }
+            }
+            if (j == n) {
+                rrow[4 * n + 0] = ci.x;
+                rrow[4 * n + 1] = ci.y;
+                rrow[4 * n + 2] = ci.z;
+                rrow[4 * n + 3] = wi;
+                n++;
+            }
+            if (is_black(ci)) any_black = true;
+        }
+    }
+    return n;
+}
+
+// skip_blacks (icbc.h:1730-1748), compacting the row in place.
+__device__ __forceinline__ int skip_blacks(float *rrow, int count) {
+    int m = 0;
+    for (int i = 0; i < count; i++) {
+        const V3 ci = texel(rrow, i);
+        const float wi = rrow[4 * i + 3];
+        if (is_black(ci)) continue;
+        rrow[4 * m + 0] = ci.x;
+        rrow[4 * m + 1] = ci.y;
+        rrow[4 * m + 2] = ci.z;
+        rrow[4 * m + 3] = wi;
+        m++;
+    }
+    return m;
+}
+
+// Principal axis: centroid, covariance, 6 power iterations (icbc.h:1755-1844).
+__device__ __forceinline__ V3 principal_axis(const float *rrow, int count) {
+    V3 centroid = v3(0.0f, 0.0f, 0.0f);
+    float total = 0.0f;
+    for (int i = 0; i < count; i++) {
+        const float w = rrow[4 * i + 3];
+        total += w;
+        centroid = centroid + texel(rrow, i) * w;
+    }
+    centroid = centroid * (1.0f / total);
+    float m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
+    for (int i = 0; i < count; i++) {
+        const V3 a = texel(rrow, i) - centroid;
+        const V3 b = a * rrow[4 * i + 3];
+        m0 += a.x * b.x; m1 += a.x * b.y; m2 += a.x * b.z;
+        m3 += a.y * b.y; m4 += a.y * b.z; m5 += a.z * b.z;
+    }
+    if (m0 == 0 && m3 == 0 && m5 == 0) return v3(0.0f, 0.0f, 0.0f);
+    const V3 row0 = v3(m0, m1, m2), row1 = v3(m1, m3, m4), row2 = v3(m2, m4, m5);
+    const float r0 = dot(row0, row0), r1 = dot(row1, row1), r2 = dot(row2, row2);
+    V3 v = (r0 > r1 && r0 > r2) ? row0 : (r1 > r2 ? row1 : row2);
+#pragma unroll
+    for (int it = 0; it < 6; it++) {
+        const float x = v.x * m0 + v.y * m1 + v.z * m2;
+        const float y = v.x * m1 + v.y * m3 + v.z * m4;
+        const float z = v.x * m2 + v.y * m4 + v.z * m5;
+        const float norm = tmax(tmax(x, y), z);
+        v = v3(x, y, z) * (1.0f / norm);
+    }
+    return v;
+}
+
+// compute_sat (icbc.h:1857-1937) into this lane's SAT row.  The stable
+// insertion sort is replaced by stable ranks (position = #smaller +
+// #equal-and-earlier), which give the same permutation for every non-NaN key;
+// keys containing NaN take a literal insertion sort.
+__device__ __forceinline__ void build_sat(const float *rrow, int count, float *srow) {
+    const V3 axis = principal_axis(rrow, count);
+    float dps[16];
+    bool has_nan = false;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        dps[i] = i < count ? dot(texel(rrow, i), axis) : 0.0f;
+        has_nan |= (i < count) && (dps[i] != dps[i]);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) srow[c * 17] = 0.0f;
+    if (!has_nan) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            if (i < count) {
+                int pos = 0;
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    pos += (j < count) && ((dps[j] < dps[i]) || (j < i && dps[j] == dps[i]));
+                const float w = rrow[4 * i + 3];
+                srow[0 * 17 + pos + 1] = rrow[4 * i + 0] * w;
+                srow[1 * 17 + pos + 1] = rrow[4 * i + 1] * w;
+                srow[2 * 17 + pos + 1] = rrow[4 * i + 2] * w;
+                srow[3 * 17 + pos + 1] = w;
+            }
+        }
+    } else {
+        int order[16];
+        float key[16];
+        for (int i = 0; i < count; i++) { order[i] = i; key[i] = dot(texel(rrow, i), axis); }
+        for (int i = 0; i < count; i++)
+            for (int j = i; j > 0 && key[j] < key[j - 1]; j--) {
+                const float t = key[j]; key[j] = key[j - 1]; key[j - 1] = t;
+                const int o = order[j]; order[j] = order[j - 1]; order[j - 1] = o;
+            }
+        for (int k = 0; k < count; k++) {
+            const int i = order[k];
+            const float w = rrow[4 * i + 3];
+            srow[0 * 17 + k + 1] = rrow[4 * i + 0] * w;
+            srow[1 * 17 + k + 1] = rrow[4 * i + 1] * w;
+            srow[2 * 17 + k + 1] = rrow[4 * i + 2] * w;
+            srow[3 * 17 + k + 1] = w;
+        }
+    }
+    for (int k = 2; k <= count; k++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) srow[c * 17 + k] = srow[c * 17 + k - 1] + srow[c * 17 + k];
+    }
+}
+
+// output_block4 (icbc.h:3257-3274): endpoints ordered col0 >= col1.
+__device__ __forceinline__ float output_block4(const WarpCtx &w, const float *row, const EncodeParams &p, V3 v0, V3 v1,
+                                               uint32_t &c0, uint32_t &c1, uint32_t &idx) {
+    uint32_t a = to565(v0, *w.T), b = to565(v1, *w.T);
+    if (a < b) { const uint32_t t = a; a = b; b = t; }
+    const PalF pal = palette_f(a, b, p.decoder, w.T->lut255);
+    c0 = a;
+    c1 = b;
+    return select_indices<4>(row, p.cw, pal, false, idx);
+}
+
+// output_block3 (icbc.h:3238-3255): endpoints ordered col0 <= col1.
+__device__ __forceinline__ float output_block3(const WarpCtx &w, const float *row, const EncodeParams &p, V3 v0, V3 v1,
+                                               uint32_t &c0, uint32_t &c1, uint32_t &idx) {
+    uint32_t a = to565(v0, *w.T), b = to565(v1, *w.T);
+    if (a > b) { const uint32_t t = a; a = b; b = t; }
+    const PalF pal = palette_f(a, b, p.decoder, w.T->lut255);
+    c0 = a;
+    c1 = b;
+    return select_indices<3>(row, p.cw, pal, p.three_color_black != 0, idx);
+}
+
+// optimize_end_points4 (icbc.h:3278-3310): unweighted least squares over the
+// 16 input texels for fixed indices.
+__device__ __forceinline__ bool optimize_end_points4(const float *row, uint32_t indices, V3 &a, V3 &b) {
+    float alpha2 = 0.0f, beta2 = 0.0f, ab = 0.0f;
+    V3 ax = v3(0.0f, 0.0f, 0.0f), bx = v3(0.0f, 0.0f, 0.0f);
+#pragma unroll 4
+    for (int i = 0; i < 16; i++) {
+        const uint32_t bits = indices >> (2 * i);
+        float beta = (float)(bits & 1);
+        if (bits & 2) beta = (1 + beta) / 3.0f;
+        const float alpha = 1.0f - beta;
+        alpha2 += alpha * alpha;
+        beta2 += beta * beta;
+        ab += alpha * beta;
+        const V3 c = texel(row, i);
+        ax = ax + c * alpha;
+        bx = bx + c * beta;
+    }
+    const float denom = alpha2 * beta2 - ab * ab;
+    if (fabsf(denom - 0.0f) < 0.0001f) return false;
+    const float factor = 1.0f / denom;
+    a = saturate((ax * beta2 - bx * ab) * factor);
+    b = saturate((bx * alpha2 - ax * ab) * factor);
+    return true;
+}
+
+// Box fit: fit_colors_bbox, inset_bbox, select_diagonal (icbc.h:3313-3368).
+__device__ __forceinline__ void box_fit(const float *colors, int count, V3 &c0, V3 &c1) {
+    c0 = v3(0.0f, 0.0f, 0.0f);
+    c1 = v3(1.0f, 1.0f, 1.0f);
+    for (int i = 0; i < count; i++) {
+        const V3 c = texel(colors, i);
+        c0 = vmax(c0, c);
+        c1 = vmin(c1, c);
+    }
+    const float bias = (8.0f / 255.0f) / 16.0f;
+    const V3 d = c0 - c1;
+    const V3 inset = saturate(v3(d.x / 16.0f - bias, d.y / 16.0f - bias, d.z / 16.0f - bias));
+    c0 = saturate(c0 - inset);
+    c1 = saturate(c1 + inset);
+    const V3 center = (c0 + c1) * 0.5f;
+    float cov_xz = 0.0f, cov_yz = 0.0f;
+    for (int i = 0; i < count; i++) {
+        const V3 t = texel(colors, i) - center;
+        cov_xz += t.x * t.z;
+        cov_yz += t.y * t.z;
+    }
+    float x0 = c0.x, y0 = c0.y, x1 = c1.x, y1 = c1.y;
+    if (cov_xz < 0) { const float t = x0; x0 = x1; x1 = t; }
+    if (cov_yz < 0) { const float t = y0; y0 = y1; y1 = t; }
+    c0 = v3(x0, y0, c0.z);
+    c1 = v3(x1, y1, c1.z);
+}
+
+// compress_dxt1_single_color_optimal (icbc.h:3519-3534) of vector3_to_color32(c).
+__device__ __forceinline__ void single_color(const DecoderTables *D, V3 c, uint32_t &c0, uint32_t &c1, uint32_t &idx) {
+    const uint32_t r = (uint32_t)(saturate(c.x) * 255 + 0.5f) & 255;
+    const uint32_t g = (uint32_t)(saturate(c.y) * 255 + 0.5f) & 255;
+    const uint32_t b = (uint32_t)(saturate(c.z) * 255 + 0.5f) & 255;
+    uint32_t a0 = ((uint32_t)D->match5[r][0] << 11) | ((uint32_t)D->match6[g][0] << 5) | D->match5[b][0];
+    uint32_t a1 = ((uint32_t)D->match5[r][1] << 11) | ((uint32_t)D->match6[g][1] << 5) | D->match5[b][1];
+    uint32_t ix = 0xaaaaaaaau;
+    if (a0 < a1) { const uint32_t t = a0; a0 = a1; a1 = t; ix ^= 0x55555555u; }
+    c0 = a0;
+    c1 = a1;
+    idx = ix;
+}
+
+__device__ __forceinline__ uint32_t add565(uint32_t c, int dr, int dg, int db) {
+    const uint32_t r = (((c >> 11) & 31) + dr) & 31;
+    const uint32_t g = (((c >> 5) & 63) + dg) & 63;
+    const uint32_t b = ((c & 31) + db) & 31;
+    return (r << 11) | (g << 5) | b;
+}
+
+// Generic nearest-of-four indices (compute_indices, icbc.h:3179-3235).
+__device__ __forceinline__ uint32_t indices_generic(const float *row, V3 cw, const PalF &pal) {
+    const V3 p0 = pal.c[0] * cw, p1 = pal.c[1] * cw, p2 = pal.c[2] * cw, p3 = pal.c[3] * cw;
+    uint32_t out = 0;
+#pragma unroll 4
+    for (int t = 0; t < 16; t++) {
+        const V3 c = texel(row, t) * cw;
+        const V3 t0 = c - p0, t1 = c - p1, t2 = c - p2, t3 = c - p3;
+        const float d0 = dot(t0, t0), d1 = dot(t1, t1), d2 = dot(t2, t2), d3 = dot(t3, t3);
+        const bool i1 = (d1 <= d0) & (d1 < d2) & (d1 < d3);
+        const bool i2 = (d2 <= d0) & (d2 <= d1) & (d2 < d3);
+        const bool i3 = (d3 <= d0) & (d3 <= d1) & (d3 <= d2);
+        out |= ((uint32_t)(i1 | i3) | ((uint32_t)(i2 | i3) << 1)) << (2 * t);
+    }
+    return out;
+}
+
+// refine_endpoints (icbc.h:3574-3651).  Indices of a step come from the
+// palette of the current best block, so they change only when a step is
+// accepted; the step's error uses the moved endpoints' palette.
+__device__ __forceinline__ float refine(const WarpCtx &w, const float *row, const EncodeParams &p, float input_error,
+                                        uint32_t &c0, uint32_t &c1, uint32_t &idx) {
+    float best = input_error;
+    int last = 0;
+    uint32_t base_idx = indices_generic(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255));
+    for (int i = 0; i < 256; i++) {
+        const int d = i & 15;
+        const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
+        uint32_t r0 = c0, r1 = c1;
+        if ((i >> 4) & 1) r0 = add565(r0, dr, dg, db);
+        else r1 = add565(r1, dr, dg, db);
+        if (!p.three_color_mode) {
+            if (r0 == r1) r1 = add565(r1, 0, 1, 0);
+            if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
+        }
+        const PalF pr = palette_f(r0, r1, p.decoder, w.T->lut255);
+        const float e = block_error(row, p.cw, pr, base_idx);
+        if (e < best) {
+            best = e;
+            c0 = r0;
+            c1 = r1;
+            idx = base_idx;
+            last = i;
+            base_idx = indices_generic(row, p.cw, pr);
+        }
+        if (i - last > 32) break;
+    }
+    return best;
+}
+
+// ---------------------------------------------------------- cluster fit --
+
+struct FitConst {
+    float r_sum, g_sum, b_sum, w_sum;
+    float w1_3, w2_3, w1_9, w4_9, w2_9;
+    V3 metric;
+};
+
+__device__ __forceinline__ FitConst fit_const(const float *S, int count, const DecoderTables *D, V3 metric) {
+    FitConst k;
+    k.r_sum = S[0 * 17 + count];
+    k.g_sum = S[1 * 17 + count];
+    k.b_sum = S[2 * 17 + count];
+    k.w_sum = S[3 * 17 + count];
+    k.w1_3 = D->w1_3; k.w2_3 = D->w2_3; k.w1_9 = D->w1_9; k.w4_9 = D->w4_9; k.w2_9 = D->w2_9;
+    k.metric = metric;
+    return k;
+}
+
+// One cluster_fit_four iteration (icbc.h:2650-2722), scalar arithmetic order.
+__device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, const FitConst &k, V3 &a, V3 &b) {
+    const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
+    V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
+    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
+    V3 x2 = v3(S[i2], S[17 + i2], S[34 + i2]);
+    const float w0 = S[51 + i0];
+    float w1 = S[51 + i1], w2 = S[51 + i2];
+    const float w3 = k.w_sum - w2;
+    x2 = x2 - x1;
+    x1 = x1 - x0;
+    w2 = w2 - w1;
+    w1 = w1 - w0;
+    const float alpha2 = w2 * k.w1_9 + (w1 * k.w4_9 + w0);
+    const float beta2 = w1 * k.w1_9 + (w2 * k.w4_9 + w3);
+    const float ab = (w1 + w2) * k.w2_9;
+    const float factor = 1.0f / (alpha2 * beta2 - ab * ab);
+    const V3 ax = v3(x2.x * k.w1_3 + (x1.x * k.w2_3 + x0.x), x2.y * k.w1_3 + (x1.y * k.w2_3 + x0.y),
+                     x2.z * k.w1_3 + (x1.z * k.w2_3 + x0.z));
+    const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
+    a = round_ept(v3((ax.x * beta2 - bx.x * ab) * factor, (ax.y * beta2 - bx.y * ab) * factor,
+                     (ax.z * beta2 - bx.z * ab) * factor));
+    b = round_ept(v3((bx.x * alpha2 - ax.x * ab) * factor, (bx.y * alpha2 - ax.y * ab) * factor,
+                     (bx.z * alpha2 - ax.z * ab) * factor));
+    const V3 e2 = v3((a.x * (b.x * ab - ax.x) - b.x * bx.x) * 2.0f, (a.y * (b.y * ab - ax.y) - b.y * bx.y) * 2.0f,
+                     (a.z * (b.z * ab - ax.z) - b.z * bx.z) * 2.0f);
+    const V3 e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + e2.x),
+                     (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + e2.y),
+                     (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + e2.z));
+    return dot(e1, k.metric);
+}
+
+// One cluster_fit_three iteration (icbc.h:2273-2323).
+__device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, const FitConst &k, V3 &a, V3 &b) {
+    const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
+    const V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
+    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
+    const float w0 = S[51 + i0];
+    float w1 = S[51 + i1];
+    const float w2 = k.w_sum - w1;
+    x1 = x1 - x0;
+    w1 = w1 - w0;
+    const float ab = w1 * 0.25f;
+    const float alpha2 = w0 + ab;
+    const float beta2 = w2 + ab;
+    const float factor = 1.0f / (alpha2 * beta2 - ab * ab);
+    const V3 ax = x0 + x1 * 0.5f;
+    const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
+    a = round_ept(v3((ax.x * beta2 - bx.x * ab) * factor, (ax.y * beta2 - bx.y * ab) * factor,
+                     (ax.z * beta2 - bx.z * ab) * factor));
+    b = round_ept(v3((bx.x * alpha2 - ax.x * ab) * factor, (bx.y * alpha2 - ax.y * ab) * factor,
+                     (bx.z * alpha2 - ax.z * ab) * factor));
+    const V3 e2 = v3((a.x * (b.x * ab - ax.x) - b.x * bx.x) * 2.0f, (a.y * (b.y * ab - ax.y) - b.y * bx.y) * 2.0f,
+                     (a.z * (b.z * ab - ax.z) - b.z * bx.z) * 2.0f);
+    const V3 e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + e2.x),
+                     (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + e2.y),
+                     (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + e2.z));
+    return dot(e1, k.metric);
+}
+
+// Warp-cooperative search of one block's combinations.  Returns the table
+// index of the first strict minimum, or -1 when no error is below FLT_MAX
+// (the reference then keeps zero endpoints).
+template <bool FOUR>
+__device__ __forceinline__ int coop_search(const WarpCtx &w, const float *S, int count, const FitConst &k) {
+    const int total = FOUR ? w.T->four_total[count - 1] : w.T->three_total[count - 1];
+    float best = FLT_MAX;
+    int best_i = 0x7fffffff;
+    for (int i = w.lane; i < total; i += 32) {
+        V3 a, b;
+        const float e = FOUR ? cf4_combo(S, w.T->four[i], k, a, b) : cf3_combo(S, w.T->three[i], k, a, b);
+        if (e < best) { best = e; best_i = i; }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        const float ob = __shfl_xor_sync(kFull, best, off);
+        const int oi = __shfl_xor_sync(kFull, best_i, off);
+        if (ob < best || (ob == best && oi < best_i)) { best = ob; best_i = oi; }
+    }
+    return best_i == 0x7fffffff ? -1 : best_i;
+}
+
+// ------------------------------------------------------------- encoder --
+
+// Encodes the warp's 32 blocks, whose texels are in w.in.  `active` marks
+// the lanes that own a real block.  c0/c1/idx hold the caller's prior output
+// bytes on entry (levels 4..9 keep them when nothing is accepted) and the
+// encoded block on return; the return value is compress_bc1's error.
+template <int L>
+__device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
+                                             uint32_t &c1, uint32_t &idx) {
+    using O = Level<L>;
+    const int lane = w.lane;
+    const float *row = w.in + lane * kInStride;
+    float *rrow = w.red + lane * kInStride;
+    float *srow = w.sat + lane * kSatStride;
+    float err = 0.0f;
+    int count = 16;
+    bool any_black = false, live = false, need4 = false;
+
+    if (active) {
+        if (O::cluster) count = reduce_colors(row, O::threshold, rrow, any_black);
+        if (O::cluster && count == 0) {
+            c0 = c1 = idx = 0;
+            err = 0.0f;
+        } else if (O::cluster && count == 1) {
+            single_color(w.D, texel(rrow, 0), c0, c1, idx);
+            err = block_error(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255), idx);
+        } else {
+            live = true;
+            err = FLT_MAX;
+            if (O::box) {
+                V3 e0, e1;
+                box_fit(O::cluster ? rrow : row, count, e0, e1);
+                err = output_block4(w, row, p, e0, e1, c0, c1, idx);
+                if (O::lsq && optimize_end_points4(row, idx, e0, e1)) {
+                    uint32_t o0, o1, oi;
+                    const float oe = output_block4(w, row, p, e0, e1, o0, o1, oi);
+                    if (oe < err) { err = oe; c0 = o0; c1 = o1; idx = oi; }
+                }
+            }
+            if (O::cluster) {
+                build_sat(rrow, count, srow);
+                need4 = true;
+            }
+        }
+    }
+
+    if (O::cluster) {
+        const V3 metric = p.cw * p.cw;
+        __syncwarp();
+        // 4-colour cluster fit, one block at a time across the warp.
+        int my4 = -1;
+        for (unsigned mask = __ballot_sync(kFull, need4); mask; mask &= mask - 1) {
+            const int bb = __ffs(mask) - 1;
+            const int cnt = __shfl_sync(kFull, count, bb);
+            const float *S = w.sat + bb * kSatStride;
+            const int k = coop_search<true>(w, S, cnt, fit_const(S, cnt, w.D, metric));
+            if (lane == bb) my4 = k;
+        }
+        uint32_t f0 = 0, f1 = 0, fi = 0;
+        float ferr = 0.0f;
+        bool need3 = false;
+        int count3 = count;
+        if (need4) {
+            V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
+            if (my4 >= 0) cf4_combo(srow, w.T->four[my4], fit_const(srow, count, w.D, metric), a, b);
+            ferr = output_block4(w, row, p, a, b, f0, f1, fi);
+            const bool use_black = any_black && p.three_color_black;
+            const bool use_three = (O::cf3_always && p.three_color_mode) ||
+                                   (O::cf3_black_only && p.three_color_mode && p.three_color_black && use_black);
+            if (use_three) {
+                if (use_black) {
+                    count3 = skip_blacks(rrow, count);
+                    if (count3) {
+                        build_sat(rrow, count3, srow);
+                        need3 = true;
+                    }
+                } else {
+                    need3 = true;
+                }
+            }
+        }
+        __syncwarp();
+        int my3 = -1;
+        for (unsigned mask = __ballot_sync(kFull, need3); mask; mask &= mask - 1) {
+            const int bb = __ffs(mask) - 1;
+            const int cnt = __shfl_sync(kFull, count3, bb);
+            const float *S = w.sat + bb * kSatStride;
+            const int k = coop_search<false>(w, S, cnt, fit_const(S, cnt, w.D, metric));
+            if (lane == bb) my3 = k;
+        }
+        if (need3) {
+            V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
+            if (my3 >= 0) cf3_combo(srow, w.T->three[my3], fit_const(srow, count3, w.D, metric), a, b);
+            uint32_t t0, t1, ti;
+            const float e3 = output_block3(w, row, p, a, b, t0, t1, ti);
+            if (e3 < ferr) { ferr = e3; f0 = t0; f1 = t1; fi = ti; }
+        }
+        if (need4 && ferr < err) { c0 = f0; c1 = f1; idx = fi; err = ferr; }
+    }
+
+    if (O::refine && live) err = refine(w, row, p, err, c0, c1, idx);
+    return err;
+}
+
+}  // namespace icbc_gpu

@@ -1,0 +1,67 @@
+// bc1_kernels.h -- launcher interface between the host API and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bc1_encode.cuh"
+
+namespace icbc_gpu {
+
+// Float-block source (the compress_bc1 layout): colors n x 16 x RGBA floats,
+// weights n x 16 floats or NULL.  Both 16-byte aligned.
+struct BlocksSrc {
+    const float *colors;
+    const float *weights;
+};
+
+// An RGBA8 image resolved for the kernels.
+struct ImageDesc {
+    const uint8_t *rgba;
+    int64_t pitch;
+    const float *weight_plane;
+    int64_t weight_pitch;
+    uint2 *out;
+    float *errors;
+    int64_t nblocks;
+    int width, height, bw;
+    int weight_mode;
+    int vec16;  // rgba and pitch are 16-byte aligned: whole rows of a block load as one uint4
+    int level, decoder, three_color_mode, three_color_black;
+    float cw[3];
+};
+
+// A warp's unit of batched work: 32 consecutive blocks of one image.
+struct BatchTask {
+    uint32_t image;
+    uint32_t first_block;
+};
+
+using BlocksLauncher = cudaError_t (*)(const GlobalTables *, const BlocksSrc &, const EncodeParams &, void *, float *,
+                                       int64_t, cudaStream_t, int);
+using ImageLauncher = cudaError_t (*)(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t, int);
+
+#define ICBC_DECLARE_LEVEL(L)                                                                                    \
+    cudaError_t launch_blocks_l##L(const GlobalTables *, const BlocksSrc &, const EncodeParams &, void *, float *, \
+                                   int64_t, cudaStream_t, int);                                                  \
+    cudaError_t launch_image_l##L(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t, int);
+ICBC_DECLARE_LEVEL(0)
+ICBC_DECLARE_LEVEL(1)
+ICBC_DECLARE_LEVEL(2)
+ICBC_DECLARE_LEVEL(3)
+ICBC_DECLARE_LEVEL(4)
+ICBC_DECLARE_LEVEL(5)
+ICBC_DECLARE_LEVEL(6)
+ICBC_DECLARE_LEVEL(7)
+ICBC_DECLARE_LEVEL(8)
+ICBC_DECLARE_LEVEL(9)
+#undef ICBC_DECLARE_LEVEL
+
+cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
+                                int *counter, cudaStream_t stream, int grid);
+int batch_ctas_per_sm();
+cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder, cudaStream_t stream);
+cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
+                            cudaStream_t stream);
+
+}  // namespace icbc_gpu

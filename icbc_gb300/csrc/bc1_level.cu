@@ -1,0 +1,108 @@
+// bc1_level.cu -- encoder kernels of one quality level.
+//
+// Compiled once per level with -DICBC_LEVEL=<0..9> so the ten
+// specialisations build in parallel.  -fmad=false keeps every multiply and
+// add separately rounded, as the reference's scalar build does.
+#include <cuda_runtime.h>
+
+#include "bc1_loaders.cuh"
+
+#ifndef ICBC_LEVEL
+#error "compile with -DICBC_LEVEL=<0..9>"
+#endif
+
+namespace icbc_gpu {
+
+// ------------------------------------------------------------- kernels --
+
+template <int L>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_blocks(const GlobalTables *G, BlocksSrc s, EncodeParams p,
+                                                                     uint2 *out, float *errors, int64_t n) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    const WarpCtx w = warp_ctx<L>(smem, T, G, p.decoder);
+    const int64_t groups = (n + 31) / 32;
+    for (int64_t g = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); g < groups;
+         g += (int64_t)gridDim.x * kWarpsPerCta) {
+        const int64_t base = g * 32;
+        const int nb = (int)(n - base < 32 ? n - base : 32);
+        __syncwarp();
+        load_float_blocks(s, base, nb, w.in, w.lane);
+        __syncwarp();
+        const bool active = w.lane < nb;
+        const int64_t b = base + w.lane;
+        uint32_t c0 = 0, c1 = 0, idx = 0;
+        if (L >= 4 && active) {
+            const uint2 prev = out[b];
+            c0 = prev.x & 0xffff;
+            c1 = prev.x >> 16;
+            idx = prev.y;
+        }
+        const float e = encode_warp<L>(w, p, active, c0, c1, idx);
+        if (active) {
+            out[b] = make_uint2(c0 | (c1 << 16), idx);
+            if (errors) errors[b] = e;
+        }
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const GlobalTables *G, ImageDesc d, EncodeParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    const WarpCtx w = warp_ctx<L>(smem, T, G, p.decoder);
+    const int64_t groups = (d.nblocks + 31) / 32;
+    for (int64_t g = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); g < groups;
+         g += (int64_t)gridDim.x * kWarpsPerCta) {
+        const int64_t b = g * 32 + w.lane;
+        const bool active = b < d.nblocks;
+        __syncwarp();
+        if (active) load_image_block(d, b, w.in + w.lane * kInStride, T.lut255);
+        __syncwarp();
+        uint32_t c0 = 0, c1 = 0, idx = 0;
+        if (L >= 4 && active) {
+            const uint2 prev = d.out[b];
+            c0 = prev.x & 0xffff;
+            c1 = prev.x >> 16;
+            idx = prev.y;
+        }
+        const float e = encode_warp<L>(w, p, active, c0, c1, idx);
+        if (active) {
+            d.out[b] = make_uint2(c0 | (c1 << 16), idx);
+            if (d.errors) d.errors[b] = e;
+        }
+    }
+}
+
+constexpr int L = ICBC_LEVEL;
+
+#define ICBC_CAT2(a, b) a##b
+#define ICBC_CAT(a, b) ICBC_CAT2(a, b)
+
+cudaError_t ICBC_CAT(launch_blocks_l, ICBC_LEVEL)(const GlobalTables *G, const BlocksSrc &s, const EncodeParams &p,
+                                                  void *out, float *errors, int64_t n, cudaStream_t stream, int sms) {
+    const size_t smem = smem_bytes(Level<L>::cluster);
+    cudaError_t e = cudaFuncSetAttribute(k_encode_blocks<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t groups = (n + 31) / 32;
+    const int64_t ctas = (groups + kWarpsPerCta - 1) / kWarpsPerCta;
+    const int grid = (int)(ctas < (int64_t)sms * 64 ? ctas : (int64_t)sms * 64);
+    k_encode_blocks<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, s, p, reinterpret_cast<uint2 *>(out), errors, n);
+    return cudaGetLastError();
+}
+
+cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
+                                                 cudaStream_t stream, int sms) {
+    const size_t smem = smem_bytes(Level<L>::cluster);
+    cudaError_t e = cudaFuncSetAttribute(k_encode_image<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t groups = (d.nblocks + 31) / 32;
+    const int64_t ctas = (groups + kWarpsPerCta - 1) / kWarpsPerCta;
+    const int grid = (int)(ctas < (int64_t)sms * 64 ? ctas : (int64_t)sms * 64);
+    k_encode_image<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p);
+    return cudaGetLastError();
+}
+
+}  // namespace icbc_gpu

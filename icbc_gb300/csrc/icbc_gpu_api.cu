@@ -1,0 +1,532 @@
+// icbc_gpu_api.cu -- host side of the C ABI declared in include/icbc_gpu.h.
+//
+// Owns the init-time tables (built here on the host, uploaded once per
+// device), validates every argument before a launch, plans batched work and
+// runs the host-buffer end-to-end path.  No exceptions cross the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/icbc_gpu.h"
+#include "bc1_kernels.h"
+
+using namespace icbc_gpu;
+
+namespace {
+
+std::mutex g_mutex;
+int g_decoder = -1;
+bool g_tables_built = false;
+GlobalTables g_host_tables;
+GlobalTables *g_dev_tables[64] = {};
+thread_local std::string t_last_error;
+
+int set_cuda_error(cudaError_t e) {
+    t_last_error = cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? ICBC_GPU_ERR_OUT_OF_MEMORY : ICBC_GPU_ERR_CUDA;
+}
+
+// Rounding thresholds between adjacent expanded 5- and 6-bit values
+// (icbc.h:1560-1570).  They are data of the BC1 encoding and must match the
+// reference literally, including the FLT_MAX sentinels.
+const float kMid5[32] = {
+    0.015686f, 0.047059f, 0.078431f, 0.111765f, 0.145098f, 0.176471f, 0.207843f, 0.241176f,
+    0.274510f, 0.305882f, 0.337255f, 0.370588f, 0.403922f, 0.435294f, 0.466667f, 0.5f,
+    0.533333f, 0.564706f, 0.596078f, 0.629412f, 0.662745f, 0.694118f, 0.725490f, 0.758824f,
+    0.792157f, 0.823529f, 0.854902f, 0.888235f, 0.921569f, 0.952941f, 0.984314f, FLT_MAX};
+const float kMid6[64] = {
+    0.007843f, 0.023529f, 0.039216f, 0.054902f, 0.070588f, 0.086275f, 0.101961f, 0.117647f,
+    0.133333f, 0.149020f, 0.164706f, 0.180392f, 0.196078f, 0.211765f, 0.227451f, 0.245098f,
+    0.262745f, 0.278431f, 0.294118f, 0.309804f, 0.325490f, 0.341176f, 0.356863f, 0.372549f,
+    0.388235f, 0.403922f, 0.419608f, 0.435294f, 0.450980f, 0.466667f, 0.482353f, 0.500000f,
+    0.517647f, 0.533333f, 0.549020f, 0.564706f, 0.580392f, 0.596078f, 0.611765f, 0.627451f,
+    0.643137f, 0.658824f, 0.674510f, 0.690196f, 0.705882f, 0.721569f, 0.737255f, 0.754902f,
+    0.772549f, 0.788235f, 0.803922f, 0.819608f, 0.835294f, 0.850980f, 0.866667f, 0.882353f,
+    0.898039f, 0.913725f, 0.929412f, 0.945098f, 0.960784f, 0.976471f, 0.992157f, FLT_MAX};
+
+// Best (max, min) endpoint pair reproducing each 8-bit value under a decoder's
+// interpolation, the error measure of PrepareOptTable5/6 (icbc.h:3377-3485):
+// D3D10 takes the worst of the AMD, NVIDIA and Intel reconstructions.  Ties
+// keep the first pair in (min, max) scan order.
+void build_match(uint8_t table[256][2], int bits, int decoder) {
+    const int levels = 1 << bits;
+    for (int v = 0; v < 256; v++) {
+        int best = 25600;
+        for (int lo = 0; lo < levels; lo++) {
+            for (int hi = 0; hi < levels; hi++) {
+                const int elo = bits == 5 ? (lo << 3) | (lo >> 2) : (lo << 2) | (lo >> 4);
+                const int ehi = bits == 5 ? (hi << 3) | (hi >> 2) : (hi << 2) | (hi >> 4);
+                const int amd = std::abs(((43 * ehi + 21 * elo + 32) >> 6) - v);
+                const int nv = std::abs((bits == 5 ? ((2 * hi + lo) * 22) / 8
+                                                   : (256 * elo + (ehi - elo) / 4 + 128 + (ehi - elo) * 80) / 256) - v);
+                const int intel = std::abs(((171 * ehi + 85 * elo + 128) >> 8) - v);
+                int err;
+                switch (decoder) {
+                    case 1: err = nv; break;
+                    case 2: err = amd; break;
+                    case 3: err = intel; break;
+                    default: err = std::max(std::max(amd, nv), intel); break;
+                }
+                if (err < best) {
+                    best = err;
+                    table[v][0] = (uint8_t)hi;
+                    table[v][1] = (uint8_t)lo;
+                }
+            }
+        }
+    }
+}
+
+// All tables, built once.  The cluster enumerations list every boundary
+// triple 0 <= c0 <= c1 <= c2 <= t (pairs c0 <= c1 <= t for three clusters),
+// except all-zero, grouped by t = 1..16 and ordered by (c0, c1) inside a
+// group -- the order icbc.h:1965-2034 produces, so a prefix serves n colours.
+void build_tables(GlobalTables &G) {
+    std::memset(&G, 0, sizeof(G));
+    SharedTables &S = G.s;
+    int i4 = 0, i3 = 0;
+    for (int t = 1; t <= 16; t++) {
+        for (int c0 = 0; c0 <= t; c0++)
+            for (int c1 = c0; c1 <= t; c1++) S.four[i4++] = (uint32_t)c0 | ((uint32_t)c1 << 8) | ((uint32_t)t << 16);
+        S.four_total[t - 1] = i4;
+        for (int c0 = 0; c0 <= t; c0++) S.three[i3++] = (uint32_t)c0 | ((uint32_t)t << 8);
+        S.three_total[t - 1] = i3;
+    }
+    for (int i = 0; i < 256; i++) S.lut255[i] = (float)i / 255.0f;
+    std::memcpy(S.mid5, kMid5, sizeof(kMid5));
+    std::memcpy(S.mid6, kMid6, sizeof(kMid6));
+    for (int d = 0; d < 4; d++) {
+        DecoderTables &D = G.dec[d];
+        // init_decoder_weights (icbc.h:3495-3515).
+        float w1_3 = 1.0f / 3, w2_3 = 2.0f / 3;
+        if (d == 2) { w1_3 = 21.0f / 64; w2_3 = 43.0f / 64; }
+        if (d == 3) { w1_3 = 85.0f / 256; w2_3 = 171.0f / 256; }
+        D.w1_3 = w1_3;
+        D.w2_3 = w2_3;
+        D.w1_9 = w1_3 * w1_3;
+        D.w4_9 = w2_3 * w2_3;
+        D.w2_9 = w1_3 * w2_3;
+        build_match(D.match5, 5, d);
+        build_match(D.match6, 6, d);
+    }
+}
+
+// Makes sure the current device holds the tables; returns them in *out.
+// The first call on a device allocates and uploads them (synchronously).
+int ensure_device_tables(const GlobalTables **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    if (dev < 0 || dev >= 64) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (g_decoder < 0) return ICBC_GPU_ERR_NOT_INITIALIZED;
+    if (!g_dev_tables[dev]) {
+        GlobalTables *d = nullptr;
+        e = cudaMalloc(&d, sizeof(GlobalTables));
+        if (e == cudaSuccess) e = cudaMemcpy(d, &g_host_tables, sizeof(GlobalTables), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            if (d) cudaFree(d);
+            return set_cuda_error(e);
+        }
+        g_dev_tables[dev] = d;
+    }
+    if (out) *out = g_dev_tables[dev];
+    return ICBC_GPU_OK;
+}
+
+const BlocksLauncher kBlocksLaunch[10] = {launch_blocks_l0, launch_blocks_l1, launch_blocks_l2, launch_blocks_l3,
+                                          launch_blocks_l4, launch_blocks_l5, launch_blocks_l6, launch_blocks_l7,
+                                          launch_blocks_l8, launch_blocks_l9};
+const ImageLauncher kImageLaunch[10] = {launch_image_l0, launch_image_l1, launch_image_l2, launch_image_l3,
+                                        launch_image_l4, launch_image_l5, launch_image_l6, launch_image_l7,
+                                        launch_image_l8, launch_image_l9};
+
+int sm_count() {
+    static int sms[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!sms[dev]) {
+        int n = 1;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev] = n > 0 ? n : 1;
+    }
+    return sms[dev];
+}
+
+int resolve_decoder(int decoder, int *out) {
+    if (decoder == ICBC_GPU_DECODER_DEFAULT) {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        decoder = g_decoder;
+        if (decoder < 0) return ICBC_GPU_ERR_NOT_INITIALIZED;
+    }
+    if (decoder < 0 || decoder > 3) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    *out = decoder;
+    return ICBC_GPU_OK;
+}
+
+bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+EncodeParams make_params(int decoder, int tc, int tcb, const float cw[3]) {
+    EncodeParams p;
+    p.decoder = decoder;
+    p.three_color_mode = tc ? 1 : 0;
+    p.three_color_black = tcb ? 1 : 0;
+    p.cw = V3{cw[0], cw[1], cw[2]};
+    return p;
+}
+
+// Validates an image descriptor and resolves it for the kernels.
+int resolve_image(const icbc_gpu_image &im, ImageDesc &d) {
+    if (!im.rgba || !im.out || im.width < 1 || im.height < 1) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (im.level < 0 || im.level > 9) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (im.weight_mode < 0 || im.weight_mode > 2) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (im.pitch < 4 * (int64_t)im.width) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(im.rgba, 4) || im.pitch % 4 || !aligned(im.out, 8)) return ICBC_GPU_ERR_MISALIGNED;
+    if (im.weight_mode == ICBC_GPU_WEIGHTS_PLANE) {
+        if (!im.weight_plane || im.weight_pitch < im.width) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+        if (!aligned(im.weight_plane, 4)) return ICBC_GPU_ERR_MISALIGNED;
+    }
+    if (im.errors && !aligned(im.errors, 4)) return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(im.decoder, &dec);
+    if (st) return st;
+    d.rgba = im.rgba;
+    d.pitch = im.pitch;
+    d.weight_plane = im.weight_plane;
+    d.weight_pitch = im.weight_pitch;
+    d.out = reinterpret_cast<uint2 *>(im.out);
+    d.errors = im.errors;
+    d.width = im.width;
+    d.height = im.height;
+    d.bw = (im.width + 3) / 4;
+    d.nblocks = (int64_t)d.bw * ((im.height + 3) / 4);
+    d.weight_mode = im.weight_mode;
+    d.vec16 = aligned(im.rgba, 16) && im.pitch % 16 == 0;
+    d.level = im.level;
+    d.decoder = dec;
+    d.three_color_mode = im.three_color_mode ? 1 : 0;
+    d.three_color_black = im.three_color_black ? 1 : 0;
+    d.cw[0] = im.color_weights[0];
+    d.cw[1] = im.color_weights[1];
+    d.cw[2] = im.color_weights[2];
+    return ICBC_GPU_OK;
+}
+
+}  // namespace
+
+// Relative cost of a 32-block task per level, used to order batched work
+// most-expensive first (cluster fit dominates from level 2 on).
+static const int kLevelCost[10] = {1, 2, 6, 8, 12, 14, 16, 17, 20, 26};
+
+struct icbc_gpu_batch {
+    ImageDesc *d_images = nullptr;
+    BatchTask *d_tasks = nullptr;
+    int *d_counter = nullptr;
+    int ntasks = 0;
+    int grid = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int icbc_gpu_init(int decoder) {
+    if (decoder < 0 || decoder > 3) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        if (!g_tables_built) {
+            build_tables(g_host_tables);
+            g_tables_built = true;
+        }
+        g_decoder = decoder;
+    }
+    return ensure_device_tables(nullptr);
+}
+
+int icbc_gpu_get_decoder(void) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    return g_decoder;
+}
+
+const char *icbc_gpu_status_string(int status) {
+    switch (status) {
+        case ICBC_GPU_OK: return "ok";
+        case ICBC_GPU_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case ICBC_GPU_ERR_NOT_INITIALIZED: return "not initialized (call icbc_gpu_init)";
+        case ICBC_GPU_ERR_CUDA: return "CUDA error";
+        case ICBC_GPU_ERR_OUT_OF_MEMORY: return "out of memory";
+        case ICBC_GPU_ERR_MISALIGNED: return "misaligned pointer or pitch";
+        case ICBC_GPU_ERR_BUDGET: return "request exceeds the memory budget";
+        case ICBC_GPU_ERR_NOT_READY: return "not ready";
+        case ICBC_GPU_ERR_CANCELLED: return "cancelled";
+        case ICBC_GPU_ERR_NOT_FOUND: return "not found";
+        default: return "unknown status";
+    }
+}
+
+const char *icbc_gpu_last_error(void) { return t_last_error.c_str(); }
+
+int icbc_gpu_sm_count(void) { return sm_count(); }
+
+int icbc_gpu_debug_tables(int decoder, uint8_t match5[512], uint8_t match6[512], float weights[5], uint32_t four[968],
+                          int32_t four_total[16], uint32_t three[152], int32_t three_total[16]) {
+    if (decoder < 0 || decoder > 3) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_tables_built) {
+        build_tables(g_host_tables);
+        g_tables_built = true;
+    }
+    const DecoderTables &D = g_host_tables.dec[decoder];
+    if (match5) std::memcpy(match5, D.match5, 512);
+    if (match6) std::memcpy(match6, D.match6, 512);
+    if (weights) {
+        weights[0] = D.w1_3; weights[1] = D.w2_3; weights[2] = D.w1_9; weights[3] = D.w4_9; weights[4] = D.w2_9;
+    }
+    if (four) std::memcpy(four, g_host_tables.s.four, 968 * sizeof(uint32_t));
+    if (four_total) std::memcpy(four_total, g_host_tables.s.four_total, sizeof(g_host_tables.s.four_total));
+    if (three) std::memcpy(three, g_host_tables.s.three, 152 * sizeof(uint32_t));
+    if (three_total) std::memcpy(three_total, g_host_tables.s.three_total, sizeof(g_host_tables.s.three_total));
+    return ICBC_GPU_OK;
+}
+
+int icbc_gpu_compress_bc1_blocks(int level, const float *d_colors, const float *d_weights, const float color_weights[3],
+                                 int three_color_mode, int three_color_black, int decoder, void *d_out,
+                                 float *d_errors, int64_t n_blocks, void *stream) {
+    if (level < 0 || level > 9 || n_blocks < 0 || !color_weights) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (n_blocks == 0) return ICBC_GPU_OK;
+    if (!d_colors || !d_out) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(d_colors, 16) || (d_weights && !aligned(d_weights, 16)) || !aligned(d_out, 8) ||
+        (d_errors && !aligned(d_errors, 4)))
+        return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(decoder, &dec);
+    if (st) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const GlobalTables *G = nullptr;
+    st = ensure_device_tables(&G);
+    if (st) return st;
+    BlocksSrc src{d_colors, d_weights};
+    cudaError_t e = kBlocksLaunch[level](G, src, make_params(dec, three_color_mode, three_color_black, color_weights),
+                                         d_out, d_errors, n_blocks, s, sm_count());
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+int icbc_gpu_compress_bc1_image(const icbc_gpu_image *image, void *stream) {
+    if (!image) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    ImageDesc d;
+    int st = resolve_image(*image, d);
+    if (st) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const GlobalTables *G = nullptr;
+    st = ensure_device_tables(&G);
+    if (st) return st;
+    cudaError_t e = kImageLaunch[d.level](G, d, make_params(d.decoder, d.three_color_mode, d.three_color_black, d.cw),
+                                          s, sm_count());
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_batch **batch) {
+    if (!batch || n_images < 0 || (n_images > 0 && !images)) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    *batch = nullptr;
+    std::vector<ImageDesc> descs((size_t)n_images);
+    for (int i = 0; i < n_images; i++) {
+        int st = resolve_image(images[i], descs[i]);
+        if (st) return st;
+        if (descs[i].nblocks > 0xffffffffLL - 32) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    }
+    const GlobalTables *G = nullptr;
+    int st = ensure_device_tables(&G);
+    if (st) return st;
+    // Tasks of 32 blocks, most expensive level first, larger images first
+    // inside a level, so the tail of the persistent launch is cheap work.
+    std::vector<int> order((size_t)n_images);
+    for (int i = 0; i < n_images; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (kLevelCost[descs[a].level] != kLevelCost[descs[b].level])
+            return kLevelCost[descs[a].level] > kLevelCost[descs[b].level];
+        return descs[a].nblocks > descs[b].nblocks;
+    });
+    std::vector<BatchTask> tasks;
+    for (int i : order)
+        for (int64_t b = 0; b < descs[i].nblocks; b += 32) tasks.push_back(BatchTask{(uint32_t)i, (uint32_t)b});
+    if (tasks.size() > 0x7fffffff) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    icbc_gpu_batch *B = new icbc_gpu_batch();
+    B->ntasks = (int)tasks.size();
+    B->grid = sm_count() * batch_ctas_per_sm();
+    cudaError_t e = cudaMalloc(&B->d_images, sizeof(ImageDesc) * std::max(1, n_images));
+    if (e == cudaSuccess) e = cudaMalloc(&B->d_tasks, sizeof(BatchTask) * std::max<size_t>(1, tasks.size()));
+    if (e == cudaSuccess) e = cudaMalloc(&B->d_counter, sizeof(int));
+    if (e == cudaSuccess && n_images)
+        e = cudaMemcpy(B->d_images, descs.data(), sizeof(ImageDesc) * n_images, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !tasks.empty())
+        e = cudaMemcpy(B->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
+    // Capture "reset the queue counter, run the persistent kernel" once.
+    cudaStream_t cs = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int), cs);
+        cudaError_t e2 = e1 == cudaSuccess && B->ntasks
+                             ? launch_encode_batch(G, B->d_images, B->d_tasks, B->ntasks, B->d_counter, cs, B->grid)
+                             : e1;
+        e = cudaStreamEndCapture(cs, &B->graph);
+        if (e1 != cudaSuccess) e = e1;
+        else if (e2 != cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&B->exec, B->graph, 0);
+    if (cs) cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+        int r = set_cuda_error(e);
+        icbc_gpu_batch_destroy(B);
+        return r;
+    }
+    *batch = B;
+    return ICBC_GPU_OK;
+}
+
+int icbc_gpu_batch_launch(icbc_gpu_batch *batch, void *stream) {
+    if (!batch || !batch->exec) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaGraphLaunch(batch->exec, reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+int icbc_gpu_batch_destroy(icbc_gpu_batch *batch) {
+    if (!batch) return ICBC_GPU_OK;
+    if (batch->exec) cudaGraphExecDestroy(batch->exec);
+    if (batch->graph) cudaGraphDestroy(batch->graph);
+    if (batch->d_images) cudaFree(batch->d_images);
+    if (batch->d_tasks) cudaFree(batch->d_tasks);
+    if (batch->d_counter) cudaFree(batch->d_counter);
+    delete batch;
+    return ICBC_GPU_OK;
+}
+
+int icbc_gpu_compress_bc1_images(const icbc_gpu_image *images, int n_images, void *stream) {
+    icbc_gpu_batch *B = nullptr;
+    int st = icbc_gpu_batch_create(images, n_images, &B);
+    if (st) return st;
+    st = icbc_gpu_batch_launch(B, stream);
+    if (!st) {
+        cudaError_t e = cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) st = set_cuda_error(e);
+    }
+    icbc_gpu_batch_destroy(B);
+    return st;
+}
+
+int icbc_gpu_decode_bc1(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks, int decoder, void *stream) {
+    if (n_blocks < 0) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (n_blocks == 0) return ICBC_GPU_OK;
+    if (!d_blocks || !d_rgba) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(d_blocks, 8) || !aligned(d_rgba, 16)) return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(decoder, &dec);
+    if (st) return st;
+    cudaError_t e = launch_decode(d_blocks, d_rgba, n_blocks, dec, reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+int icbc_gpu_evaluate_bc1_error(const uint8_t *d_rgba, const void *d_blocks, float *d_errors, int64_t n_blocks,
+                                int decoder, void *stream) {
+    if (n_blocks < 0) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (n_blocks == 0) return ICBC_GPU_OK;
+    if (!d_blocks || !d_rgba || !d_errors) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(d_blocks, 8) || !aligned(d_rgba, 16) || !aligned(d_errors, 4)) return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(decoder, &dec);
+    if (st) return st;
+    cudaError_t e = launch_evaluate(d_rgba, d_blocks, d_errors, n_blocks, dec, reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+// Device buffers of the host-buffer path, grown on demand and reused.
+namespace {
+struct HostPath {
+    std::mutex m;
+    cudaStream_t stream = nullptr;
+    void *d_img = nullptr;
+    size_t img_bytes = 0;
+    void *d_out = nullptr;
+    size_t out_bytes = 0;
+    float *d_err = nullptr;
+    size_t err_bytes = 0;
+    float *d_plane = nullptr;
+    size_t plane_bytes = 0;
+};
+HostPath g_host_path;
+
+cudaError_t grow(void **p, size_t *have, size_t need) {
+    if (*have >= need) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    cudaError_t e = cudaMalloc(p, need);
+    if (e == cudaSuccess) *have = need;
+    return e;
+}
+}  // namespace
+
+int icbc_gpu_compress_bc1_image_host(const uint8_t *rgba, int32_t width, int32_t height, int64_t pitch,
+                                     int32_t weight_mode, const float *weight_plane, int32_t level, int32_t decoder,
+                                     int32_t three_color_mode, int32_t three_color_black, const float color_weights[3],
+                                     void *out, float *errors) {
+    if (!rgba || !out || !color_weights || width < 1 || height < 1 || pitch < 4 * (int64_t)width)
+        return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (weight_mode == ICBC_GPU_WEIGHTS_PLANE && !weight_plane) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    HostPath &H = g_host_path;
+    std::lock_guard<std::mutex> lock(H.m);
+    cudaError_t e = cudaSuccess;
+    if (!H.stream) e = cudaStreamCreateWithFlags(&H.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    const int64_t nb = (int64_t)((width + 3) / 4) * ((height + 3) / 4);
+    const int64_t dpitch = ((4 * (int64_t)width + 15) / 16) * 16;
+    e = grow(&H.d_img, &H.img_bytes, (size_t)(dpitch * height));
+    if (e == cudaSuccess) e = grow(&H.d_out, &H.out_bytes, (size_t)(nb * 8));
+    if (e == cudaSuccess && errors) e = grow(reinterpret_cast<void **>(&H.d_err), &H.err_bytes, (size_t)(nb * 4));
+    if (e == cudaSuccess && weight_mode == ICBC_GPU_WEIGHTS_PLANE)
+        e = grow(reinterpret_cast<void **>(&H.d_plane), &H.plane_bytes, sizeof(float) * (size_t)width * height);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    e = cudaMemcpy2DAsync(H.d_img, (size_t)dpitch, rgba, (size_t)pitch, 4 * (size_t)width, (size_t)height,
+                          cudaMemcpyHostToDevice, H.stream);
+    if (e == cudaSuccess && weight_mode == ICBC_GPU_WEIGHTS_PLANE)
+        e = cudaMemcpyAsync(H.d_plane, weight_plane, sizeof(float) * (size_t)width * height, cudaMemcpyHostToDevice,
+                            H.stream);
+    if (e != cudaSuccess) return set_cuda_error(e);
+    icbc_gpu_image im;
+    std::memset(&im, 0, sizeof(im));
+    im.rgba = reinterpret_cast<const uint8_t *>(H.d_img);
+    im.width = width;
+    im.height = height;
+    im.pitch = dpitch;
+    im.weight_mode = weight_mode;
+    im.weight_plane = H.d_plane;
+    im.weight_pitch = width;
+    im.level = level;
+    im.decoder = decoder;
+    im.three_color_mode = three_color_mode;
+    im.three_color_black = three_color_black;
+    im.color_weights[0] = color_weights[0];
+    im.color_weights[1] = color_weights[1];
+    im.color_weights[2] = color_weights[2];
+    im.out = H.d_out;
+    im.errors = errors ? H.d_err : nullptr;
+    if (level >= 4) {
+        e = cudaMemcpyAsync(H.d_out, out, (size_t)nb * 8, cudaMemcpyHostToDevice, H.stream);
+        if (e != cudaSuccess) return set_cuda_error(e);
+    }
+    int st = icbc_gpu_compress_bc1_image(&im, H.stream);
+    if (st) return st;
+    e = cudaMemcpyAsync(out, H.d_out, (size_t)nb * 8, cudaMemcpyDeviceToHost, H.stream);
+    if (e == cudaSuccess && errors)
+        e = cudaMemcpyAsync(errors, H.d_err, (size_t)nb * 4, cudaMemcpyDeviceToHost, H.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(H.stream);
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+}  // extern "C"

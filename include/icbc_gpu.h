@@ -1,0 +1,167 @@
+/*
+ * icbc_gpu.h -- C ABI of the GB300 (sm_103a) BC1 encoder.
+ *
+ * Drop-in for the compress path of icbc (icbc.h v1.05): the same encoder,
+ * bit-exact with the reference's scalar build, run as CUDA kernels over many
+ * blocks at once.  Plain C types only: pointers, sizes, ints and floats.
+ * Every entry point returns an icbc_gpu_status; nothing throws across the ABI.
+ *
+ * Pointers documented as "device" are CUDA device (or managed) memory owned by
+ * the caller; "host" pointers are ordinary host memory.  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  Calls that
+ * take a stream are asynchronous unless stated otherwise.
+ *
+ * Block layout (icbc.h:234-258): 8 bytes, little-endian
+ *   u16 col0 (RGB565, r<<11 | g<<5 | b), u16 col1, u32 indices (texel i in bits 2i..2i+1).
+ * Texel order inside a block is row-major: texel i = (x = i % 4, y = i / 4).
+ */
+#ifndef ICBC_GPU_H
+#define ICBC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum icbc_gpu_status {
+    ICBC_GPU_OK = 0,
+    ICBC_GPU_ERR_INVALID_ARGUMENT = 1, /* bad level, decoder, size, flag or NULL pointer */
+    ICBC_GPU_ERR_NOT_INITIALIZED = 2,  /* icbc_gpu_init has not run */
+    ICBC_GPU_ERR_CUDA = 3,             /* a CUDA runtime call failed; see icbc_gpu_last_error */
+    ICBC_GPU_ERR_OUT_OF_MEMORY = 4,    /* a device or pinned allocation failed */
+    ICBC_GPU_ERR_MISALIGNED = 5,       /* a pointer or pitch breaks the documented alignment */
+    ICBC_GPU_ERR_BUDGET = 6,           /* serving: request larger than the HBM budget */
+    ICBC_GPU_ERR_NOT_READY = 7,        /* serving: result not finished yet */
+    ICBC_GPU_ERR_CANCELLED = 8,        /* serving: request cancelled or server stopped */
+    ICBC_GPU_ERR_NOT_FOUND = 9         /* serving: unknown request id */
+};
+
+/* Hardware decoders (values of icbc::Decoder, icbc.h:12-17). */
+enum icbc_gpu_decoder {
+    ICBC_GPU_DECODER_DEFAULT = -1,     /* the decoder chosen by icbc_gpu_init */
+    ICBC_GPU_DECODER_D3D10 = 0,
+    ICBC_GPU_DECODER_NVIDIA = 1,
+    ICBC_GPU_DECODER_AMD = 2,
+    ICBC_GPU_DECODER_INTEL = 3
+};
+
+/* Quality levels are icbc::Quality (icbc.h:21-36): 0..9, Fast = 1,
+ * Default = 8, Max = 9. */
+#define ICBC_GPU_QUALITY_FAST 1
+#define ICBC_GPU_QUALITY_DEFAULT 8
+#define ICBC_GPU_QUALITY_MAX 9
+
+/* Where the per-texel input_weights of an RGBA8 image come from. */
+enum icbc_gpu_weight_mode {
+    ICBC_GPU_WEIGHTS_UNIFORM = 0,      /* 1.0f for every texel (icbc_test.cpp:405) */
+    ICBC_GPU_WEIGHTS_ALPHA = 1,        /* alpha / 255.0f */
+    ICBC_GPU_WEIGHTS_PLANE = 2         /* a float plane of width x height */
+};
+
+/* Uploads the init-time tables for all four decoders and selects `decoder`
+ * as the default.  Replaces icbc::init (icbc.h:19, :3813-3818).  Safe to call
+ * again (only the default decoder changes); serialised by an internal lock.
+ * Must not race with encodes that use ICBC_GPU_DECODER_DEFAULT. */
+int icbc_gpu_init(int decoder);
+
+/* The default decoder, or -1 before icbc_gpu_init. */
+int icbc_gpu_get_decoder(void);
+
+/* Short text for a status code; the last CUDA error text of this thread. */
+const char *icbc_gpu_status_string(int status);
+const char *icbc_gpu_last_error(void);
+
+/* Encodes n_blocks independent blocks.  Replaces n calls of
+ * icbc::compress_bc1 (icbc.h:48, :3846-3848), each with the same arguments:
+ *   d_colors  device, n_blocks x 16 texels x RGBA float (alpha ignored),
+ *             16-byte aligned;
+ *   d_weights device, n_blocks x 16 floats, 16-byte aligned, or NULL for 1.0f;
+ *   color_weights host, 3 floats (the reference's color_weights[3]);
+ *   d_out     device, n_blocks x 8 bytes, 8-byte aligned.  At levels 4..9 a
+ *             block whose search finds no finite error keeps the bytes that
+ *             were there, as the reference leaves its output untouched;
+ *   d_errors  device, n_blocks floats or NULL: the value icbc::compress_bc1
+ *             returns for each block (its weighted error).
+ * decoder is ICBC_GPU_DECODER_DEFAULT or 0..3; level is 0..9. */
+int icbc_gpu_compress_bc1_blocks(int level, const float *d_colors, const float *d_weights,
+                                 const float color_weights[3], int three_color_mode,
+                                 int three_color_black, int decoder, void *d_out, float *d_errors,
+                                 int64_t n_blocks, void *stream);
+
+/* One RGBA8 image and how to encode it. */
+typedef struct icbc_gpu_image {
+    const uint8_t *rgba;        /* device, RGBA8 rows */
+    int32_t width, height;      /* >= 1 */
+    int64_t pitch;              /* bytes between rows, >= 4 * width */
+    int32_t weight_mode;        /* icbc_gpu_weight_mode */
+    const float *weight_plane;  /* device, used with ICBC_GPU_WEIGHTS_PLANE */
+    int64_t weight_pitch;       /* floats between weight-plane rows */
+    int32_t level;              /* 0..9 */
+    int32_t decoder;            /* ICBC_GPU_DECODER_DEFAULT or 0..3 */
+    int32_t three_color_mode;
+    int32_t three_color_black;
+    float color_weights[3];
+    void *out;                  /* device, ceil(w/4) * ceil(h/4) * 8 bytes, 8-byte aligned */
+    float *errors;              /* device, one float per block, or NULL */
+} icbc_gpu_image;
+
+/* Encodes one image (plain form: one kernel launch).  Blocks are written in
+ * row-major block order; partial blocks at the right and bottom edges
+ * replicate the last column / row.  Texels convert as u8 / 255.0f with alpha
+ * 1.0f, as icbc_test.cpp:398-406 does before calling compress_bc1. */
+int icbc_gpu_compress_bc1_image(const icbc_gpu_image *image, void *stream);
+
+/* Batched form: many images of any size, level and decoder in one persistent
+ * launch that drains a device work queue of (image, block range) tiles,
+ * largest cost first.  A batch is planned once and can be launched many
+ * times (the launch is a captured CUDA graph).  The image descriptors are
+ * copied at create time; the pixel and output buffers they point to must stay
+ * valid while the batch is launched. */
+typedef struct icbc_gpu_batch icbc_gpu_batch;
+int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_batch **batch);
+int icbc_gpu_batch_launch(icbc_gpu_batch *batch, void *stream);
+int icbc_gpu_batch_destroy(icbc_gpu_batch *batch);
+/* Convenience: create, launch on `stream`, synchronise, destroy. */
+int icbc_gpu_compress_bc1_images(const icbc_gpu_image *images, int n_images, void *stream);
+
+/* Decodes n blocks to RGBA8 texels (64 bytes per block).  Replaces
+ * icbc::decode_bc1 (icbc.h:38, :2915-2927). */
+int icbc_gpu_decode_bc1(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks, int decoder,
+                        void *stream);
+
+/* Unweighted squared RGB error of n blocks against their RGBA8 texels
+ * (64 bytes per block).  Replaces icbc::evaluate_bc1_error (icbc.h:43,
+ * :3030-3046). */
+int icbc_gpu_evaluate_bc1_error(const uint8_t *d_rgba, const void *d_blocks, float *d_errors,
+                                int64_t n_blocks, int decoder, void *stream);
+
+/* End-to-end call with HOST buffers: copies the image in, encodes, copies the
+ * blocks (and errors if non-NULL) out, and returns when they are on the host.
+ * rgba is host memory (pitch bytes per row), weight_plane host floats
+ * (width per row) or NULL.  Synchronous. */
+int icbc_gpu_compress_bc1_image_host(const uint8_t *rgba, int32_t width, int32_t height, int64_t pitch,
+                                     int32_t weight_mode, const float *weight_plane, int32_t level,
+                                     int32_t decoder, int32_t three_color_mode, int32_t three_color_black,
+                                     const float color_weights[3], void *out, float *errors);
+
+/* Number of SMs of the current device (for sizing host-side work). */
+int icbc_gpu_sm_count(void);
+
+/* Diagnostics, host only (no CUDA call): copies the init-time tables the
+ * library builds -- the single-colour match tables of a decoder
+ * (s_match5/s_match6, icbc.h:3374-3375, as [256][2] {max, min}), its cluster
+ * weights {w1_3, w2_3, w1_9, w4_9, w2_9} (icbc.h:1961-1962) and the cluster
+ * enumerations packed c0 | c1 << 8 | c2 << 16 with their prefix totals
+ * (icbc.h:1947-1950).  Any output pointer may be NULL. */
+int icbc_gpu_debug_tables(int decoder, uint8_t match5[512], uint8_t match6[512], float weights[5],
+                          uint32_t four[968], int32_t four_total[16], uint32_t three[152],
+                          int32_t three_total[16]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ICBC_GPU_H */

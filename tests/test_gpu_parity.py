@@ -1,0 +1,212 @@
+"""GPU: the sm_103a kernels against the oracle and the reference's golden
+vectors.  Integer/byte outputs must be bit-identical, and so must the float
+error each block returns (the arithmetic is the reference's, operation for
+operation), so every comparison here is exact equality."""
+import os
+
+import numpy as np
+import pytest
+
+from icbc_gb300 import synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FLAGS = ((1, 1), (1, 0), (0, 0))
+CWS = ((1.0, 1.0, 1.0), (0.299, 0.587, 0.114))
+
+
+def same_bits(a, b):
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
+
+
+@pytest.mark.parametrize("level", range(10))
+def test_blocks_match_golden(gpu_lib, level):
+    ig = gpu_lib
+    g = np.load(os.path.join(GOLDEN, "blocks.npz"))
+    colors, wr = g["colors"], g["weights_rand"]
+    wu = np.ones_like(wr)
+    for dec in range(4):
+        for tc, tcb in FLAGS:
+            for wn, wt in (("u", wu), ("r", wr)):
+                cw = CWS[(dec + (wn == "r")) % 2]
+                key = "L%d_D%d_tc%d_tcb%d_w%s" % (level, dec, tc, tcb, wn)
+                b, e = ig.compress_blocks(colors, wt, level, dec, cw, tc, tcb)
+                assert np.array_equal(b, g[key + "_blocks"]), key
+                assert same_bits(e, g[key + "_errors"]), key
+
+
+@pytest.mark.parametrize("level", range(10))
+def test_blocks_match_oracle_mixture(gpu_lib, level):
+    ig = gpu_lib
+    cols, w = synth.mixed_blocks(6000, seed=200 + level)
+    for dec in range(4):
+        cw = CWS[dec % 2]
+        b, e = ig.compress_blocks(cols, w, level, dec, cw, True, True)
+        ob, oe = O.compress_blocks(cols, w, level, dec, cw, True, True, nthreads=8)
+        bad = np.nonzero((b != ob).any(1))[0]
+        assert bad.size == 0, (level, dec, bad[:10])
+        assert same_bits(e, oe)
+
+
+def test_default_decoder_follows_init(gpu_lib):
+    ig = gpu_lib
+    cols, w = synth.mixed_blocks(500, seed=17)
+    try:
+        for dec in range(4):
+            ig.init(dec)
+            b, e = ig.compress_blocks(cols, w, 8, ig.DECODER_DEFAULT, (1, 1, 1), True, True)
+            ob, oe = O.compress_blocks(cols, w, 8, dec, (1, 1, 1), True, True)
+            assert np.array_equal(b, ob) and same_bits(e, oe)
+    finally:
+        ig.init(ig.Decoder_D3D10)
+
+
+def test_single_block_api(gpu_lib):
+    ig = gpu_lib
+    cols, w = synth.mixed_blocks(40, seed=21)
+    for i in range(40):
+        out = bytearray(8)
+        err = ig.compress_bc1(9, cols[i], w[i], (1, 1, 1), True, True, out)
+        ob, oe = O.compress_blocks(cols[i:i + 1], w[i:i + 1], 9, 0, (1, 1, 1), True, True)
+        assert bytes(out) == bytes(ob[0]) and same_bits(err, oe[0])
+
+
+def _to_dev(img):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(img)).cuda()
+
+
+def test_image512_quality_default_golden(gpu_lib):
+    ig = gpu_lib
+    g = np.load(os.path.join(GOLDEN, "image512.npz"))
+    img = synth.gradient_noise_rects(512, 512, 0)
+    out, err = ig.compress_image(_to_dev(img), 8, 0, (1, 1, 1), with_errors=True)
+    assert np.array_equal(out.cpu().numpy(), g["blocks"])
+    assert same_bits(err.cpu().numpy(), g["errors"])
+
+
+@pytest.mark.parametrize("level", range(10))
+def test_image_alpha_weights_all_levels(gpu_lib, level):
+    ig = gpu_lib
+    img = synth.quality_sweep_image(256, 192, seed=5)
+    cw = (0.299, 0.587, 0.114)
+    for dec in (0, 1, 2, 3):
+        out, err = ig.compress_image(_to_dev(img), level, dec, cw, weight_mode=ig.WEIGHTS_ALPHA, with_errors=True)
+        ob, oe = O.encode_image(img, level, dec, cw, 1, None, True, True, nthreads=8)
+        assert np.array_equal(out.cpu().numpy(), ob), (level, dec)
+        assert same_bits(err.cpu().numpy(), oe)
+
+
+@pytest.mark.parametrize("size", [(1, 1), (3, 5), (5, 3), (4, 4), (7, 9), (130, 66), (66, 130), (33, 1)])
+def test_image_edge_sizes(gpu_lib, size):
+    ig = gpu_lib
+    w, h = size
+    img = synth.hard_mixture_image(w, h, seed=w * 100 + h)
+    for level in (0, 1, 4, 8, 9):
+        out = ig.compress_image(_to_dev(img), level, 0, (1, 1, 1), weight_mode=ig.WEIGHTS_ALPHA)
+        ob, _ = O.encode_image(img, level, 0, (1, 1, 1), 1, None, True, True)
+        assert np.array_equal(out.cpu().numpy(), ob), (size, level)
+
+
+def test_image_unaligned_pitch_and_weight_plane(gpu_lib):
+    import torch
+    ig = gpu_lib
+    img = synth.gradient_noise_rects(61, 47, seed=8)
+    # rows padded to an odd number of pixels: pitch not a multiple of 16 bytes
+    padded = np.zeros((47, 63, 4), np.uint8)
+    padded[:, :61] = img
+    dev = torch.from_numpy(padded).cuda()
+    plane = (synth.uniform(3, 0, (47, 61)) * 2).astype(np.float32)
+    plane[::3, ::2] = 0
+    dplane = torch.from_numpy(plane).cuda()
+    nb = ig.blocks_of(61, 47)
+    out = torch.zeros((nb, 8), dtype=torch.uint8, device="cuda")
+    d = ig.image_desc(dev, 9, out, None, 1, (1, 1, 1), ig.WEIGHTS_PLANE, dplane, width=61, height=47,
+                      pitch=63 * 4)
+    import ctypes
+    ig._check(ig.load().icbc_gpu_compress_bc1_image(ctypes.byref(d), ig._stream_ptr()), "image")
+    torch.cuda.synchronize()
+    ob, _ = O.encode_image(img, 9, 1, (1, 1, 1), 2, plane, True, True)
+    assert np.array_equal(out.cpu().numpy(), ob)
+
+
+def test_prior_output_kept_when_no_finite_error(gpu_lib):
+    ig = gpu_lib
+    cols, _ = synth.mixed_blocks(300, seed=9)
+    w = np.full((300, 16), 3e38, np.float32)
+    prior = np.arange(300 * 8, dtype=np.uint8).reshape(300, 8)
+    for level in (4, 8, 9):
+        b, e = ig.compress_blocks(cols, w, level, 0, (1, 1, 1), True, True, initial=prior)
+        ob, oe = O.compress_blocks(cols, w, level, 0, (1, 1, 1), True, True, out=prior)
+        assert np.array_equal(b, ob) and same_bits(e, oe)
+
+
+def test_batch_matches_plain_and_oracle(gpu_lib):
+    import torch
+    ig = gpu_lib
+    specs = synth.batch_specs(40, seed=5, lo=8, hi=300)
+    imgs, outs, descs, plain = [], [], [], []
+    for s in specs:
+        img = synth.gradient_noise_rects(s.width, s.height, s.seed)
+        dev = _to_dev(img)
+        nb = ig.blocks_of(s.width, s.height)
+        out = torch.zeros((nb, 8), dtype=torch.uint8, device="cuda")
+        imgs.append((img, dev))
+        outs.append(out)
+        descs.append(ig.image_desc(dev, s.level, out, None, s.decoder))
+        plain.append(ig.compress_image(dev, s.level, s.decoder))
+    batch = ig.Batch(descs)
+    for _ in range(2):  # a planned batch relaunches (graph replay) with the same result
+        batch.launch()
+        torch.cuda.synchronize()
+        for (img, _), s, out, p in zip(imgs, specs, outs, plain):
+            assert np.array_equal(out.cpu().numpy(), p.cpu().numpy()), (s.width, s.height, s.level)
+    batch.close()
+    for (img, _), s, out in list(zip(imgs, specs, outs))[::5]:
+        ob, _ = O.encode_image(img, s.level, s.decoder, (1, 1, 1), 0, None, True, True, nthreads=8)
+        assert np.array_equal(out.cpu().numpy(), ob)
+
+
+def test_decode_evaluate_golden(gpu_lib):
+    import torch
+    ig = gpu_lib
+    g = np.load(os.path.join(GOLDEN, "decode.npz"))
+    blocks = torch.from_numpy(g["blocks"]).cuda()
+    rgba = torch.from_numpy(g["rgba"]).cuda()
+    for d in range(4):
+        assert np.array_equal(ig.decode_blocks(blocks, d).cpu().numpy(), g["decoded_D%d" % d])
+        assert same_bits(ig.evaluate_errors(rgba, blocks, d).cpu().numpy(), g["error_D%d" % d])
+
+
+def test_host_buffer_path(gpu_lib):
+    ig = gpu_lib
+    img = synth.quality_sweep_image(200, 120, seed=2)
+    for level in (1, 8):
+        errs = np.zeros(ig.blocks_of(200, 120), np.float32)
+        out = ig.compress_image_host(img, level, 0, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA, errors=errs)
+        ob, oe = O.encode_image(img, level, 0, (0.299, 0.587, 0.114), 1, None, True, True)
+        assert np.array_equal(out, ob) and same_bits(errs, oe)
+
+
+@pytest.mark.parametrize("level", [0, 8, 9])
+def test_full_size_sampled_parity(gpu_lib, level):
+    """4096x4096 quality-sweep image: every 61st block checked against the
+    oracle, plus decode->evaluate consistency over the whole image."""
+    import torch
+    ig = gpu_lib
+    img = synth.quality_sweep_image(4096, 4096, seed=1)
+    cw = (0.299, 0.587, 0.114)
+    out = ig.compress_image(_to_dev(img), level, 0, cw, weight_mode=ig.WEIGHTS_ALPHA)
+    blocks = out.cpu().numpy()
+    cols, w, tex = O.image_blocks(img, weight_mode=1)
+    idx = np.arange(0, blocks.shape[0], 61)
+    ob, _ = O.compress_blocks(cols[idx], w[idx], level, 0, cw, True, True, nthreads=8)
+    assert np.array_equal(blocks[idx], ob)
+    # whole image: GPU decode + evaluate equals the oracle's on a sample, and PSNR is sane
+    rgba = torch.from_numpy(np.ascontiguousarray(tex.reshape(-1, 64))).cuda()
+    e = ig.evaluate_errors(rgba, out, 0).cpu().numpy()
+    oe = O.evaluate_bc1_error(tex[idx].reshape(-1, 64), blocks[idx], 0)
+    assert same_bits(e[idx], oe)
+    mse = e.astype(np.float64).sum() / (16 * blocks.shape[0])
+    assert 20 * np.log10(255 / np.sqrt(mse)) > 30

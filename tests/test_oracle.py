@@ -1,0 +1,95 @@
+"""CPU: the oracle against the reference's golden vectors and, where the
+reference checkout exists, against the compiled reference itself."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from icbc_gb300 import synth
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FLAGS = ((1, 1), (1, 0), (0, 0))
+CWS = ((1.0, 1.0, 1.0), (0.299, 0.587, 0.114))
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(os.path.join(GOLDEN, "blocks.npz"))
+
+
+@pytest.mark.parametrize("level", range(10))
+def test_oracle_matches_golden_blocks(golden, level):
+    colors, wr = golden["colors"], golden["weights_rand"]
+    wu = np.ones_like(wr)
+    for dec in range(4):
+        for tc, tcb in FLAGS:
+            for wn, wt in (("u", wu), ("r", wr)):
+                cw = CWS[(dec + (wn == "r")) % 2]
+                key = "L%d_D%d_tc%d_tcb%d_w%s" % (level, dec, tc, tcb, wn)
+                b, e = O.compress_blocks(colors, wt, level, dec, cw, tc, tcb)
+                assert np.array_equal(b, golden[key + "_blocks"]), key
+                assert np.array_equal(e.view(np.uint32), golden[key + "_errors"].view(np.uint32)), key
+
+
+def test_oracle_matches_golden_image():
+    g = np.load(os.path.join(GOLDEN, "image512.npz"))
+    img = synth.gradient_noise_rects(512, 512, 0)
+    assert hashlib.sha256(img.tobytes()).digest() == g["sha256"].tobytes(), "generator output changed"
+    b, e = O.encode_image(img, 8, 0, (1, 1, 1), 0, None, True, True, nthreads=4)
+    assert np.array_equal(b, g["blocks"])
+    assert np.array_equal(e.view(np.uint32), g["errors"].view(np.uint32))
+
+
+def test_oracle_decode_evaluate_golden():
+    g = np.load(os.path.join(GOLDEN, "decode.npz"))
+    for d in range(4):
+        assert np.array_equal(O.decode_bc1(g["blocks"], d), g["decoded_D%d" % d])
+        e = O.evaluate_bc1_error(g["rgba"], g["blocks"], d)
+        assert np.array_equal(e.view(np.uint32), g["error_D%d" % d].view(np.uint32))
+
+
+def test_image_path_equals_block_path():
+    """Image encode (edge replication, u8/255, alpha weights) equals the block
+    API on the gathered texels, for a size that is not a multiple of 4."""
+    img = synth.quality_sweep_image(70, 45, seed=3)
+    cols, w, _ = O.image_blocks(img, weight_mode=1)
+    for level in (0, 5, 9):
+        b1, e1 = O.encode_image(img, level, 2, (0.299, 0.587, 0.114), 1, None, True, True)
+        b2, e2 = O.compress_blocks(cols, w, level, 2, (0.299, 0.587, 0.114), True, True)
+        assert np.array_equal(b1, b2) and np.array_equal(e1, e2)
+
+
+def test_threaded_equals_single():
+    cols, w = synth.mixed_blocks(3000, seed=8)
+    b1, e1 = O.compress_blocks(cols, w, 9, 1, (1, 1, 1), True, True, nthreads=1)
+    b8, e8 = O.compress_blocks(cols, w, 9, 1, (1, 1, 1), True, True, nthreads=8)
+    assert np.array_equal(b1, b8) and np.array_equal(e1, e8)
+
+
+@pytest.mark.skipif(O.ref() is None, reason="reference checkout not available")
+@pytest.mark.parametrize("level", range(10))
+def test_oracle_matches_compiled_reference(level):
+    cols, w = synth.mixed_blocks(1500, seed=100 + level)
+    for dec in range(4):
+        for tc, tcb in FLAGS:
+            cw = CWS[dec % 2]
+            a, ea = O.compress_blocks(cols, w, level, dec, cw, tc, tcb)
+            b, eb = O.ref_compress_blocks(cols, w, level, dec, cw, tc, tcb)
+            assert np.array_equal(a, b), (level, dec, tc, tcb)
+            assert np.array_equal(ea.view(np.uint32), eb.view(np.uint32)), (level, dec, tc, tcb)
+
+
+@pytest.mark.skipif(O.ref() is None, reason="reference checkout not available")
+def test_oracle_prior_output_semantics():
+    """Weights so large the cluster-fit error overflows: the reference keeps the
+    caller's prior bytes at levels 4..9; so must the oracle."""
+    cols, _ = synth.mixed_blocks(200, seed=9)
+    w = np.full((200, 16), 3e38, np.float32)
+    prior = np.arange(200 * 8, dtype=np.uint8).reshape(200, 8)
+    for level in (4, 8, 9):
+        a, ea = O.compress_blocks(cols, w, level, 0, (1, 1, 1), True, True, out=prior)
+        b, eb = O.ref_compress_blocks(cols, w, level, 0, (1, 1, 1), True, True, out=prior)
+        assert np.array_equal(a, b)
+        assert np.array_equal(ea.view(np.uint32), eb.view(np.uint32))
