@@ -64,4 +64,9 @@ cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder
 cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
                             cudaStream_t stream);
 
+// Host-side services of icbc_gpu_api.cu used by other translation units.
+const GlobalTables &host_tables();
+int level_cost(int level);
+int current_sm_count();
+
 }  // namespace icbc_gpu

@@ -220,9 +220,31 @@ int resolve_image(const icbc_gpu_image &im, ImageDesc &d) {
 
 }  // namespace
 
+namespace icbc_gpu {
+
+// Host-side services shared with other translation units of the library.
+const GlobalTables &host_tables() {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_tables_built) {
+        build_tables(g_host_tables);
+        g_tables_built = true;
+    }
+    return g_host_tables;
+}
+
+int resolve_image_desc(const icbc_gpu_image &image, ImageDesc &desc) { return resolve_image(image, desc); }
+
+int current_sm_count() { return sm_count(); }
+
+}  // namespace icbc_gpu
+
 // Relative cost of a 32-block task per level, used to order batched work
 // most-expensive first (cluster fit dominates from level 2 on).
 static const int kLevelCost[10] = {1, 2, 6, 8, 12, 14, 16, 17, 20, 26};
+
+namespace icbc_gpu {
+int level_cost(int level) { return kLevelCost[level < 0 ? 0 : level > 9 ? 9 : level]; }
+}  // namespace icbc_gpu
 
 struct icbc_gpu_batch {
     ImageDesc *d_images = nullptr;

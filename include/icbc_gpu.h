@@ -127,6 +127,35 @@ int icbc_gpu_batch_destroy(icbc_gpu_batch *batch);
 /* Convenience: create, launch on `stream`, synchronise, destroy. */
 int icbc_gpu_compress_bc1_images(const icbc_gpu_image *images, int n_images, void *stream);
 
+/* Largest batch icbc_gpu_compress_bc1_images_noalloc accepts. */
+#define ICBC_GPU_NOALLOC_MAX_IMAGES 256
+
+/* Batched encode that allocates nothing.  No counterpart in the reference:
+ * icbc encodes one block per call on the CPU and owns no device memory.
+ *
+ * For callers that may not allocate device memory -- an engine or texture
+ * streamer that reserves the whole device budget itself, code running inside
+ * such an allocator, or a latency-critical path that cannot pay for
+ * cudaMalloc/cudaFree, which can synchronise the device.  Encodes up to
+ * ICBC_GPU_NOALLOC_MAX_IMAGES images of any size, level and decoder, with the
+ * same output as icbc_gpu_compress_bc1_images, and calls no cudaMalloc,
+ * cudaFree or other allocating routine: its work queue (image descriptors,
+ * task offsets, queue counter) lives in one fixed array inside this library's
+ * device code, about 38 KB with its tables, which every GPU that loads the
+ * library holds until the process exits.  Inputs and outputs are the
+ * caller's device buffers, as for icbc_gpu_compress_bc1_image.
+ *   - More than ICBC_GPU_NOALLOC_MAX_IMAGES images: ICBC_GPU_ERR_INVALID_ARGUMENT,
+ *     returned before any device work.
+ *   - The first call on a device sets that device up (looks up the array's
+ *     address, uploads the tables) synchronously, with the device current;
+ *     make that first call before any stream capture.  icbc_gpu_init is not
+ *     needed unless an image uses ICBC_GPU_DECODER_DEFAULT.
+ *   - Asynchronous on `stream`; `images` may be reused once the call returns.
+ *   - Every call shares the one array and each call clears its queue counter.
+ *     Calls whose GPU work overlaps (unordered streams, concurrent host
+ *     threads) race on the array and corrupt each other: order them. */
+int icbc_gpu_compress_bc1_images_noalloc(const icbc_gpu_image *images, int n_images, void *stream);
+
 /* Decodes n blocks to RGBA8 texels (64 bytes per block).  Replaces
  * icbc::decode_bc1 (icbc.h:38, :2915-2927). */
 int icbc_gpu_decode_bc1(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks, int decoder,
