@@ -143,10 +143,11 @@ def sample_rows(img: np.ndarray, stride: int) -> np.ndarray:
     return np.ascontiguousarray(np.concatenate(rows, axis=0))
 
 
-def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=LEVELS):
+def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=None):
     """Times the oracle (CPU restatement of the reference encoder) on the sample."""
     from oracle import oracle as O
     O.lib()  # build/load outside the timed region
+    levels = LEVELS if levels is None else levels
     times, stats, outs = {}, {}, {}
     for lv in levels:
         t0 = time.perf_counter()
@@ -178,7 +179,7 @@ def run_reference(args):
     step_times = []
     per_level = {lv: [] for lv in LEVELS}
     for _ in range(args.steps):
-        times, _, _ = cpu_sweep(sample, nthreads)
+        times, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS)
         step_times.append(sum(times.values()))
         for lv in LEVELS:
             per_level[lv].append(times[lv])
@@ -266,28 +267,22 @@ def run_ours(args):
     value = ws * len(LEVELS) * px / (step_ms * 1e-3) / 1e9
 
     # End to end through the host-buffer C-ABI call: pinned image in, blocks out.
-    pin = torch.from_numpy(img).pin_memory()
-    host_img = pin.numpy()
-    host_out = {lv: torch.zeros((nb, 8), dtype=torch.uint8).pin_memory().numpy() for lv in LEVELS}
-    for lv in LEVELS:
-        ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
-    e2e_steps = max(2, min(args.steps, 5))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        for lv in LEVELS:
-            ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
-    e2e_t = (time.perf_counter() - t0) / e2e_steps
-    e2e_value = ws * len(LEVELS) * px / e2e_t / 1e9
-    h2d = len(LEVELS) * img.nbytes + sum(nb * 8 for lv in LEVELS if lv >= 4)
-    d2h = len(LEVELS) * nb * 8
-
+    e2e_value = h2d = d2h = None
+    if not args.no_e2e:
+        e2e_value, h2d, d2h = e2e_leg(ig, torch, img, nb, px, ws, args)
     if rank != 0:
+        return
+    batch = None if (args.no_batch or args.no_cpu_baseline) else batch_leg(ig, torch, dev, args)
+    if args.no_cpu_baseline:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": step_ms, "levels": LEVELS,
+                          "per_level_ms": lvl_ms, "e2e": e2e_value, "clocks": clk, "profiling_run": True}))
         return
     # CPU baseline + algorithmic op counts + sampled parity on every level.
     sample = sample_rows(img, args.cpu_stride)
     sample_px = sample.shape[0] * sample.shape[1]
     nthreads = os.cpu_count() or 1
-    ctimes, cstats, couts = cpu_sweep(sample, nthreads)
+    ctimes, cstats, couts = cpu_sweep(sample, nthreads, levels=LEVELS)
     cpu_value = len(LEVELS) * sample_px / sum(ctimes.values()) / 1e9
     bw = w // 4
     rows = list(range(0, h // 4, args.cpu_stride))
@@ -295,7 +290,7 @@ def run_ours(args):
     for lv in LEVELS:
         gpu = outs[lv].cpu().numpy().reshape(h // 4, bw, 8)[rows].reshape(-1, 8)
         mismatches[str(lv)] = int((gpu != couts[lv]).any(1).sum())
-    scale = nb / sum(s["blocks"] for s in [cstats[0]])
+    scale = nb / cstats[LEVELS[0]]["blocks"]
     ops = {lv: algorithmic_ops(cstats[lv], lv) * scale for lv in LEVELS}
     peaks = load_peaks()
     peak = fp32_peak_tops(peaks, sms)
@@ -321,18 +316,102 @@ def run_ours(args):
                      "unit": "Tops/s", "frac": achieved / peak, "traffic": None,
                      "peak_source": "128 FP32 lanes x %d SMs x %s MHz (%s sm_max_mhz)" % (
                          sms, peaks.get("sm_max_mhz"), peaks["source"])},
-        "roofline_hbm_level0": {"bound": "hbm", "achieved": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9, "peak": hbm,
-                                "unit": "GB/s", "frac": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9 / hbm,
-                                "traffic": None},
+        "roofline_hbm_level0": ({"bound": "hbm", "achieved": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9, "peak": hbm,
+                                 "unit": "GB/s", "frac": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9 / hbm,
+                                 "traffic": None} if 0 in lvl_ms else None),
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": "every %dth block row (%d px) at all 10 levels" % (args.cpu_stride, sample_px)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step"},
+        "batch": batch,
         "gpu_launches": args.steps * len(LEVELS),
         "clocks": clk,
         "wall_s_timed": wall,
     }
     print(json.dumps(line))
+
+
+def e2e_leg(ig, torch, img, nb, px, ws, args):
+    """Same metric through the host-buffer C-ABI call: pinned image in, blocks
+    out, host<->device copies inside the timed region."""
+    pin = torch.from_numpy(img).pin_memory()
+    host_img = pin.numpy()
+    host_out = {lv: torch.zeros((nb, 8), dtype=torch.uint8).pin_memory().numpy() for lv in LEVELS}
+    for lv in LEVELS:
+        ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
+    steps = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for lv in LEVELS:
+            ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
+    t = (time.perf_counter() - t0) / steps
+    h2d = len(LEVELS) * img.nbytes + sum(nb * 8 for lv in LEVELS if lv >= 4)
+    d2h = len(LEVELS) * nb * 8
+    return ws * len(LEVELS) * px / t / 1e9, h2d, d2h
+
+
+def batch_leg(ig, torch, dev, args):
+    """Mixed-size batch: 2,000 images (sides log-uniform 64..2048, 10% not
+    multiples of 4), random level 0..9 and decoder D3D10/NVIDIA/AMD, uniform
+    weights, cw {1,1,1}.  Content: crops of gradient/noise/rectangle textures.
+    Times the plain form (one launch per image) against the batched form
+    (one persistent launch, replayed graph), checks both give the same bytes."""
+    from icbc_gb300 import synth
+    specs = synth.batch_specs(args.batch_images, seed=7)
+    bases = [torch.from_numpy(synth.gradient_noise_rects(2048, 2048, 100 + k)).to(dev) for k in range(4)]
+    imgs, outs_plain, outs_batch, descs = [], [], [], []
+    px = 0
+    for i, s in enumerate(specs):
+        base = bases[i % len(bases)]
+        y0 = (s.seed * 131) % (2049 - s.height)
+        x0 = (s.seed * 197) % (2049 - s.width)
+        img = base[y0:y0 + s.height, x0:x0 + s.width].contiguous()
+        nb = ig.blocks_of(s.width, s.height)
+        imgs.append(img)
+        outs_plain.append(torch.zeros((nb, 8), dtype=torch.uint8, device=dev))
+        ob = torch.zeros((nb, 8), dtype=torch.uint8, device=dev)
+        outs_batch.append(ob)
+        descs.append(ig.image_desc(img, s.level, ob, None, s.decoder))
+        px += s.width * s.height
+    del bases
+    stream = torch.cuda.Stream(device=dev)
+    plain_descs = [ig.image_desc(img, s.level, o, None, s.decoder) for s, img, o in zip(specs, imgs, outs_plain)]
+
+    def plain():
+        ig.compress_images_each(plain_descs, stream)
+
+    batch = ig.Batch(descs)
+    with torch.cuda.stream(stream):
+        plain()
+        batch.launch(stream)
+    torch.cuda.synchronize()
+    same = all(torch.equal(a, b) for a, b in zip(outs_plain, outs_batch))
+    res = {}
+    for name, fn in (("plain", plain), ("batched", lambda: batch.launch(stream))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            fn()
+            e0.record(stream)
+            for _ in range(args.batch_steps):
+                fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.batch_steps
+        res[name] = {"ms": ms, "gpix_s": px / (ms * 1e-3) / 1e9}
+    batch.close()
+    # spot-check a few images against the oracle
+    from oracle import oracle as O
+    bad = 0
+    for i in range(0, len(specs), max(1, len(specs) // 6)):
+        s = specs[i]
+        ob, _ = O.encode_image(imgs[i].cpu().numpy(), s.level, s.decoder, (1, 1, 1), 0, None, True, True,
+                               nthreads=os.cpu_count() or 1)
+        bad += int((outs_batch[i].cpu().numpy() != ob).any(1).sum())
+    return {"workload": "mixed_batch_%d_images" % len(specs), "pixels": px,
+            "plain": res["plain"], "batched": res["batched"],
+            "speedup_batched_over_plain": res["plain"]["ms"] / res["batched"]["ms"],
+            "batched_equals_plain": bool(same), "oracle_mismatches_sampled": bad,
+            "launches_plain": len(specs), "launches_batched": 1}
 
 
 def main():
@@ -343,7 +422,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--cpu-stride", type=int, default=8)
+    ap.add_argument("--levels", type=int, nargs="+", default=None,
+                    help="encode only these levels (profiling); the headline uses all ten")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
+    ap.add_argument("--batch-images", type=int, default=2000)
+    ap.add_argument("--batch-steps", type=int, default=3)
     args = ap.parse_args()
+    if args.levels:
+        global LEVELS
+        LEVELS = sorted(set(args.levels))
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -81,6 +81,7 @@ def load(build_if_missing: bool = True):
             "icbc_gpu_batch_launch": (i32, [vp, vp]),
             "icbc_gpu_batch_destroy": (i32, [vp]),
             "icbc_gpu_compress_bc1_images": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
+            "icbc_gpu_compress_bc1_images_each": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
             "icbc_gpu_decode_bc1": (i32, [vp, vp, i64, i32, vp]),
             "icbc_gpu_evaluate_bc1_error": (i32, [vp, vp, vp, i64, i32, vp]),
             "icbc_gpu_compress_bc1_image_host": (i32, [vp, i32, i32, i64, i32, vp, i32, i32, i32, i32, f32p, vp, vp]),
@@ -293,6 +294,12 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def compress_images_each(descs: Sequence[ImageDesc], stream=None):
+    """Plain form over many images: one launch per image, looped in native code."""
+    arr = (ImageDesc * len(descs))(*descs)
+    _check(load().icbc_gpu_compress_bc1_images_each(arr, len(descs), _stream_ptr(stream)), "compress_bc1_images_each")
 
 
 def decode_blocks(blocks, decoder: int = Decoder_D3D10, stream=None):

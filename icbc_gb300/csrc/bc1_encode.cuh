@@ -13,8 +13,10 @@
 // Shared memory per warp, [32 blocks][odd stride] so that per-lane rows are
 // conflict-free and one block's SAT can be read by all lanes at once:
 //   in    [32][65]  texels r,g,b (float) + weight, 16 x 4 floats
-//   red   [32][65]  reduced colours + weights (reduce_colors / skip_blacks)
-//   sat   [32][69]  SAT with a leading zero: comp c at [c*17 + 0..16]
+//   sat   [32][69]  first the reduced colours + weights (reduce_colors, 16 x 4),
+//                   then, built in place through registers, the SAT with a
+//                   leading zero: component c at [c*17 + 0..16]
+// 17 KB per warp: three 4-warp CTAs per SM at levels 2..9.
 #pragma once
 
 #include "bc1_device.cuh"
@@ -27,7 +29,7 @@ constexpr int kSatStride = 69;
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr size_t kWarpFloatsLow = 32 * kInStride;                                  // L0, L1
-constexpr size_t kWarpFloatsHigh = 32 * kInStride * 2 + 32 * kSatStride;          // L2..L9
+constexpr size_t kWarpFloatsHigh = 32 * kInStride + 32 * kSatStride;              // L2..L9
 
 __host__ __device__ constexpr size_t smem_bytes(bool cluster_fit) {
     return sizeof(SharedTables) + kWarpsPerCta * 4 * (cluster_fit ? kWarpFloatsHigh : kWarpFloatsLow);
@@ -65,14 +67,13 @@ struct WarpCtx {
     const SharedTables *T;
     const DecoderTables *D;
     float *in;
-    float *red;
     float *sat;
     int lane;
 };
 
 // ------------------------------------------------------------ per lane --
 
-// reduce_colors (icbc.h:1683-1728) into this lane's `red` row.
+// reduce_colors (icbc.h:1683-1728) into rrow (the lane's SAT row, as scratch).
 __device__ __forceinline__ int reduce_colors(const float *row, float threshold, float *rrow, bool &any_black) {
     int n = 0;
     any_black = false;
@@ -106,106 +107,124 @@ __device__ __forceinline__ int reduce_colors(const float *row, float threshold, 
     return n;
 }
 
-// skip_blacks (icbc.h:1730-1748), compacting the row in place.
-__device__ __forceinline__ int skip_blacks(float *rrow, int count) {
-    int m = 0;
-    for (int i = 0; i < count; i++) {
-        const V3 ci = texel(rrow, i);
-        const float wi = rrow[4 * i + 3];
-        if (is_black(ci)) continue;
-        rrow[4 * m + 0] = ci.x;
-        rrow[4 * m + 1] = ci.y;
-        rrow[4 * m + 2] = ci.z;
-        rrow[4 * m + 3] = wi;
-        m++;
+// compute_sat (icbc.h:1857-1937) in place: the reduced colours in the lane's
+// SAT row are read into registers, then the row is overwritten with the SAT.
+// With skip_black the colours skip_blacks (icbc.h:1730-1748) would drop are
+// masked out instead of compacted (order among the rest is unchanged, so
+// every sum runs in the reference's order).  Returns the number of colours
+// in the table (0: nothing left).
+//   centroid, covariance, power iterations: icbc.h:1755-1844
+//   stable insertion sort along the axis: replaced by stable ranks
+//     (position = #smaller + #equal-and-earlier), the same permutation for
+//     every non-NaN key; keys containing NaN take a literal insertion sort.
+__device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool skip_black) {
+    float cx[16], cy[16], cz[16], cw[16];
+    unsigned use = 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const bool in = i < count;
+        cx[i] = in ? srow[4 * i + 0] : 0.0f;
+        cy[i] = in ? srow[4 * i + 1] : 0.0f;
+        cz[i] = in ? srow[4 * i + 2] : 0.0f;
+        cw[i] = in ? srow[4 * i + 3] : 0.0f;
+        if (in && !(skip_black && is_black(v3(cx[i], cy[i], cz[i])))) use |= 1u << i;
     }
-    return m;
-}
-
-// Principal axis: centroid, covariance, 6 power iterations (icbc.h:1755-1844).
-__device__ __forceinline__ V3 principal_axis(const float *rrow, int count) {
+    const int m = __popc(use);
+    if (m == 0) return 0;
     V3 centroid = v3(0.0f, 0.0f, 0.0f);
     float total = 0.0f;
-    for (int i = 0; i < count; i++) {
-        const float w = rrow[4 * i + 3];
-        total += w;
-        centroid = centroid + texel(rrow, i) * w;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        if (use & (1u << i)) {
+            total += cw[i];
+            centroid = centroid + v3(cx[i], cy[i], cz[i]) * cw[i];
+        }
     }
     centroid = centroid * (1.0f / total);
     float m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
-    for (int i = 0; i < count; i++) {
-        const V3 a = texel(rrow, i) - centroid;
-        const V3 b = a * rrow[4 * i + 3];
-        m0 += a.x * b.x; m1 += a.x * b.y; m2 += a.x * b.z;
-        m3 += a.y * b.y; m4 += a.y * b.z; m5 += a.z * b.z;
-    }
-    if (m0 == 0 && m3 == 0 && m5 == 0) return v3(0.0f, 0.0f, 0.0f);
-    const V3 row0 = v3(m0, m1, m2), row1 = v3(m1, m3, m4), row2 = v3(m2, m4, m5);
-    const float r0 = dot(row0, row0), r1 = dot(row1, row1), r2 = dot(row2, row2);
-    V3 v = (r0 > r1 && r0 > r2) ? row0 : (r1 > r2 ? row1 : row2);
 #pragma unroll
-    for (int it = 0; it < 6; it++) {
-        const float x = v.x * m0 + v.y * m1 + v.z * m2;
-        const float y = v.x * m1 + v.y * m3 + v.z * m4;
-        const float z = v.x * m2 + v.y * m4 + v.z * m5;
-        const float norm = tmax(tmax(x, y), z);
-        v = v3(x, y, z) * (1.0f / norm);
+    for (int i = 0; i < 16; i++) {
+        if (use & (1u << i)) {
+            const V3 a = v3(cx[i], cy[i], cz[i]) - centroid;
+            const V3 b = a * cw[i];
+            m0 += a.x * b.x; m1 += a.x * b.y; m2 += a.x * b.z;
+            m3 += a.y * b.y; m4 += a.y * b.z; m5 += a.z * b.z;
+        }
     }
-    return v;
-}
-
-// compute_sat (icbc.h:1857-1937) into this lane's SAT row.  The stable
-// insertion sort is replaced by stable ranks (position = #smaller +
-// #equal-and-earlier), which give the same permutation for every non-NaN key;
-// keys containing NaN take a literal insertion sort.
-__device__ __forceinline__ void build_sat(const float *rrow, int count, float *srow) {
-    const V3 axis = principal_axis(rrow, count);
+    V3 axis = v3(0.0f, 0.0f, 0.0f);
+    if (!(m0 == 0 && m3 == 0 && m5 == 0)) {
+        const V3 row0 = v3(m0, m1, m2), row1 = v3(m1, m3, m4), row2 = v3(m2, m4, m5);
+        const float r0 = dot(row0, row0), r1 = dot(row1, row1), r2 = dot(row2, row2);
+        V3 v = (r0 > r1 && r0 > r2) ? row0 : (r1 > r2 ? row1 : row2);
+#pragma unroll
+        for (int it = 0; it < 6; it++) {
+            const float x = v.x * m0 + v.y * m1 + v.z * m2;
+            const float y = v.x * m1 + v.y * m3 + v.z * m4;
+            const float z = v.x * m2 + v.y * m4 + v.z * m5;
+            const float norm = tmax(tmax(x, y), z);
+            v = v3(x, y, z) * (1.0f / norm);
+        }
+        axis = v;
+    }
     float dps[16];
     bool has_nan = false;
 #pragma unroll
     for (int i = 0; i < 16; i++) {
-        dps[i] = i < count ? dot(texel(rrow, i), axis) : 0.0f;
-        has_nan |= (i < count) && (dps[i] != dps[i]);
+        dps[i] = dot(v3(cx[i], cy[i], cz[i]), axis);
+        has_nan |= ((use >> i) & 1) && (dps[i] != dps[i]);
     }
 #pragma unroll
     for (int c = 0; c < 4; c++) srow[c * 17] = 0.0f;
     if (!has_nan) {
 #pragma unroll
         for (int i = 0; i < 16; i++) {
-            if (i < count) {
+            if (use & (1u << i)) {
                 int pos = 0;
 #pragma unroll
                 for (int j = 0; j < 16; j++)
-                    pos += (j < count) && ((dps[j] < dps[i]) || (j < i && dps[j] == dps[i]));
-                const float w = rrow[4 * i + 3];
-                srow[0 * 17 + pos + 1] = rrow[4 * i + 0] * w;
-                srow[1 * 17 + pos + 1] = rrow[4 * i + 1] * w;
-                srow[2 * 17 + pos + 1] = rrow[4 * i + 2] * w;
-                srow[3 * 17 + pos + 1] = w;
+                    pos += ((use >> j) & 1) && ((dps[j] < dps[i]) || (j < i && dps[j] == dps[i]));
+                srow[0 * 17 + pos + 1] = cx[i] * cw[i];
+                srow[1 * 17 + pos + 1] = cy[i] * cw[i];
+                srow[2 * 17 + pos + 1] = cz[i] * cw[i];
+                srow[3 * 17 + pos + 1] = cw[i];
             }
         }
     } else {
+        // Literal stable insertion sort of the kept colours (NaN keys).  The
+        // colours are copied to a local array first so that the dynamic
+        // indexing here does not move the register arrays to local memory.
+        float lc[64];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            lc[4 * i + 0] = cx[i];
+            lc[4 * i + 1] = cy[i];
+            lc[4 * i + 2] = cz[i];
+            lc[4 * i + 3] = cw[i];
+        }
         int order[16];
         float key[16];
-        for (int i = 0; i < count; i++) { order[i] = i; key[i] = dot(texel(rrow, i), axis); }
-        for (int i = 0; i < count; i++)
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            if (use & (1u << i)) { order[k] = i; key[k] = dps[i]; k++; }
+        for (int i = 0; i < m; i++)
             for (int j = i; j > 0 && key[j] < key[j - 1]; j--) {
                 const float t = key[j]; key[j] = key[j - 1]; key[j - 1] = t;
                 const int o = order[j]; order[j] = order[j - 1]; order[j - 1] = o;
             }
-        for (int k = 0; k < count; k++) {
-            const int i = order[k];
-            const float w = rrow[4 * i + 3];
-            srow[0 * 17 + k + 1] = rrow[4 * i + 0] * w;
-            srow[1 * 17 + k + 1] = rrow[4 * i + 1] * w;
-            srow[2 * 17 + k + 1] = rrow[4 * i + 2] * w;
-            srow[3 * 17 + k + 1] = w;
+        for (int q = 0; q < m; q++) {
+            const float *c = lc + 4 * order[q];
+            srow[0 * 17 + q + 1] = c[0] * c[3];
+            srow[1 * 17 + q + 1] = c[1] * c[3];
+            srow[2 * 17 + q + 1] = c[2] * c[3];
+            srow[3 * 17 + q + 1] = c[3];
         }
     }
-    for (int k = 2; k <= count; k++) {
+    for (int k = 2; k <= m; k++) {
 #pragma unroll
         for (int c = 0; c < 4; c++) srow[c * 17 + k] = srow[c * 17 + k - 1] + srow[c * 17 + k];
     }
+    return m;
 }
 
 // output_block4 (icbc.h:3257-3274): endpoints ordered col0 >= col1.
@@ -442,10 +461,15 @@ __device__ __forceinline__ int coop_search(const WarpCtx &w, const float *S, int
     const int total = FOUR ? w.T->four_total[count - 1] : w.T->three_total[count - 1];
     float best = FLT_MAX;
     int best_i = 0x7fffffff;
-    for (int i = w.lane; i < total; i += 32) {
+    // Two combinations per lane per iteration (independent dependency chains).
+    // Past the end the second one repeats the first, which a strict < never keeps.
+    for (int i = w.lane; i < total; i += 64) {
+        const int j = i + 32 < total ? i + 32 : i;
         V3 a, b;
-        const float e = FOUR ? cf4_combo(S, w.T->four[i], k, a, b) : cf3_combo(S, w.T->three[i], k, a, b);
-        if (e < best) { best = e; best_i = i; }
+        const float ei = FOUR ? cf4_combo(S, w.T->four[i], k, a, b) : cf3_combo(S, w.T->three[i], k, a, b);
+        const float ej = FOUR ? cf4_combo(S, w.T->four[j], k, a, b) : cf3_combo(S, w.T->three[j], k, a, b);
+        if (ei < best) { best = ei; best_i = i; }
+        if (ej < best) { best = ej; best_i = j; }
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
@@ -468,26 +492,25 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
     using O = Level<L>;
     const int lane = w.lane;
     const float *row = w.in + lane * kInStride;
-    float *rrow = w.red + lane * kInStride;
     float *srow = w.sat + lane * kSatStride;
     float err = 0.0f;
     int count = 16;
     bool any_black = false, live = false, need4 = false;
 
     if (active) {
-        if (O::cluster) count = reduce_colors(row, O::threshold, rrow, any_black);
+        if (O::cluster) count = reduce_colors(row, O::threshold, srow, any_black);
         if (O::cluster && count == 0) {
             c0 = c1 = idx = 0;
             err = 0.0f;
         } else if (O::cluster && count == 1) {
-            single_color(w.D, texel(rrow, 0), c0, c1, idx);
+            single_color(w.D, texel(srow, 0), c0, c1, idx);
             err = block_error(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255), idx);
         } else {
             live = true;
             err = FLT_MAX;
             if (O::box) {
                 V3 e0, e1;
-                box_fit(O::cluster ? rrow : row, count, e0, e1);
+                box_fit(O::cluster ? srow : row, count, e0, e1);
                 err = output_block4(w, row, p, e0, e1, c0, c1, idx);
                 if (O::lsq && optimize_end_points4(row, idx, e0, e1)) {
                     uint32_t o0, o1, oi;
@@ -496,7 +519,7 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
                 }
             }
             if (O::cluster) {
-                build_sat(rrow, count, srow);
+                build_sat_inplace(srow, count, false);
                 need4 = true;
             }
         }
@@ -514,6 +537,7 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
             const int k = coop_search<true>(w, S, cnt, fit_const(S, cnt, w.D, metric));
             if (lane == bb) my4 = k;
         }
+        __syncwarp();
         uint32_t f0 = 0, f1 = 0, fi = 0;
         float ferr = 0.0f;
         bool need3 = false;
@@ -527,11 +551,12 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
                                    (O::cf3_black_only && p.three_color_mode && p.three_color_black && use_black);
             if (use_three) {
                 if (use_black) {
-                    count3 = skip_blacks(rrow, count);
-                    if (count3) {
-                        build_sat(rrow, count3, srow);
-                        need3 = true;
-                    }
+                    // The reduced colours were overwritten by the SAT: reduce again,
+                    // then build the table of the non-black ones.
+                    bool ab;
+                    reduce_colors(row, O::threshold, srow, ab);
+                    count3 = build_sat_inplace(srow, count, true);
+                    need3 = count3 > 0;
                 } else {
                     need3 = true;
                 }

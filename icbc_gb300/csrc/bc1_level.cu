@@ -78,6 +78,31 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const Global
 
 constexpr int L = ICBC_LEVEL;
 
+// CTAs for n blocks.  Levels 0-1 cost the same for every block: the grid is
+// exactly the resident CTAs (from the occupancy API), each warp striding
+// over groups of 32 blocks, so there is no partial last wave and the per-CTA
+// table staging is paid once per resident CTA.  Levels 2-9 cost depends on
+// the data: two groups per warp and many CTAs, balanced by the hardware.
+template <class K>
+static int grid_for(K kernel, int64_t n, int sms) {
+    const int64_t groups = (n + 31) / 32;
+    const int64_t per_cta = (int64_t)kWarpsPerCta * (Level<L>::cluster ? 2 : 1);
+    int64_t ctas = (groups + per_cta - 1) / per_cta;
+    if (!Level<L>::cluster) {
+        static int resident = 0;
+        if (!resident) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerCta * 32,
+                                                              smem_bytes(false)) != cudaSuccess || per_sm < 1)
+                per_sm = 1;
+            resident = per_sm;
+        }
+        const int64_t cap = (int64_t)sms * resident;
+        ctas = ctas < cap ? ctas : cap;
+    }
+    return (int)(ctas < 0x7fffffff ? ctas : 0x7fffffff);
+}
+
 #define ICBC_CAT2(a, b) a##b
 #define ICBC_CAT(a, b) ICBC_CAT2(a, b)
 
@@ -86,9 +111,7 @@ cudaError_t ICBC_CAT(launch_blocks_l, ICBC_LEVEL)(const GlobalTables *G, const B
     const size_t smem = smem_bytes(Level<L>::cluster);
     cudaError_t e = cudaFuncSetAttribute(k_encode_blocks<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t groups = (n + 31) / 32;
-    const int64_t ctas = (groups + kWarpsPerCta - 1) / kWarpsPerCta;
-    const int grid = (int)(ctas < (int64_t)sms * 64 ? ctas : (int64_t)sms * 64);
+    const int grid = grid_for(k_encode_blocks<L>, n, sms);
     k_encode_blocks<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, s, p, reinterpret_cast<uint2 *>(out), errors, n);
     return cudaGetLastError();
 }
@@ -98,9 +121,7 @@ cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const Im
     const size_t smem = smem_bytes(Level<L>::cluster);
     cudaError_t e = cudaFuncSetAttribute(k_encode_image<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t groups = (d.nblocks + 31) / 32;
-    const int64_t ctas = (groups + kWarpsPerCta - 1) / kWarpsPerCta;
-    const int grid = (int)(ctas < (int64_t)sms * 64 ? ctas : (int64_t)sms * 64);
+    const int grid = grid_for(k_encode_image<L>, d.nblocks, sms);
     k_encode_image<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p);
     return cudaGetLastError();
 }

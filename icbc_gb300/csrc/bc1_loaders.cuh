@@ -90,8 +90,7 @@ __device__ __forceinline__ WarpCtx warp_ctx(unsigned char *smem, const SharedTab
     w.T = &T;
     w.D = &G->dec[decoder];
     w.in = base;
-    w.red = base + 32 * kInStride;
-    w.sat = base + 64 * kInStride;
+    w.sat = base + 32 * kInStride;
     w.lane = threadIdx.x & 31;
     return w;
 }

@@ -442,6 +442,15 @@ int icbc_gpu_compress_bc1_images(const icbc_gpu_image *images, int n_images, voi
     return st;
 }
 
+int icbc_gpu_compress_bc1_images_each(const icbc_gpu_image *images, int n_images, void *stream) {
+    if (n_images < 0 || (n_images > 0 && !images)) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n_images; i++) {
+        const int st = icbc_gpu_compress_bc1_image(&images[i], stream);
+        if (st) return st;
+    }
+    return ICBC_GPU_OK;
+}
+
 int icbc_gpu_decode_bc1(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks, int decoder, void *stream) {
     if (n_blocks < 0) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     if (n_blocks == 0) return ICBC_GPU_OK;

@@ -127,6 +127,12 @@ int icbc_gpu_batch_destroy(icbc_gpu_batch *batch);
 /* Convenience: create, launch on `stream`, synchronise, destroy. */
 int icbc_gpu_compress_bc1_images(const icbc_gpu_image *images, int n_images, void *stream);
 
+/* Plain form over many images: one kernel launch per image, in order, on
+ * `stream` (what a caller looping over icbc_gpu_compress_bc1_image gets,
+ * without per-call host overhead).  The reference for the batched form's
+ * speed-up; same output. */
+int icbc_gpu_compress_bc1_images_each(const icbc_gpu_image *images, int n_images, void *stream);
+
 /* Largest batch icbc_gpu_compress_bc1_images_noalloc accepts. */
 #define ICBC_GPU_NOALLOC_MAX_IMAGES 256
 
