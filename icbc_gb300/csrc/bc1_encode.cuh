@@ -16,6 +16,8 @@
 //   sat   [32][69]  first the reduced colours + weights (reduce_colors, 16 x 4),
 //                   then, built in place through registers, the SAT with a
 //                   leading zero: component c at [c*17 + 0..16]
+//   slots [32]      u64 per block: best (error, table index) of a cluster search
+// The pad word [68] of each SAT row holds the block's search bookkeeping.
 // 17 KB per warp: three 4-warp CTAs per SM at levels 2..9.
 #pragma once
 
@@ -29,7 +31,7 @@ constexpr int kSatStride = 69;
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr size_t kWarpFloatsLow = 32 * kInStride;                                  // L0, L1
-constexpr size_t kWarpFloatsHigh = 32 * kInStride + 32 * kSatStride;              // L2..L9
+constexpr size_t kWarpFloatsHigh = 32 * kInStride + 32 * kSatStride + 64;         // L2..L9
 
 __host__ __device__ constexpr size_t smem_bytes(bool cluster_fit) {
     return sizeof(SharedTables) + kWarpsPerCta * 4 * (cluster_fit ? kWarpFloatsHigh : kWarpFloatsLow);
@@ -68,6 +70,7 @@ struct WarpCtx {
     const DecoderTables *D;
     float *in;
     float *sat;
+    unsigned long long *slots;
     int lane;
 };
 
@@ -176,17 +179,28 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
 #pragma unroll
     for (int c = 0; c < 4; c++) srow[c * 17] = 0.0f;
     if (!has_nan) {
+        // Stable ranks from the 120 pairs i < j: j sorts before i iff
+        // dps[j] < dps[i]; otherwise i (the earlier one) sorts before j.
+        int pos[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) pos[i] = 0;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+#pragma unroll
+            for (int j = i + 1; j < 16; j++) {
+                const bool both = ((use >> i) & (use >> j) & 1) != 0;
+                const bool j_first = dps[j] < dps[i];
+                pos[i] += both && j_first;
+                pos[j] += both && !j_first;
+            }
+        }
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             if (use & (1u << i)) {
-                int pos = 0;
-#pragma unroll
-                for (int j = 0; j < 16; j++)
-                    pos += ((use >> j) & 1) && ((dps[j] < dps[i]) || (j < i && dps[j] == dps[i]));
-                srow[0 * 17 + pos + 1] = cx[i] * cw[i];
-                srow[1 * 17 + pos + 1] = cy[i] * cw[i];
-                srow[2 * 17 + pos + 1] = cz[i] * cw[i];
-                srow[3 * 17 + pos + 1] = cw[i];
+                srow[0 * 17 + pos[i] + 1] = cx[i] * cw[i];
+                srow[1 * 17 + pos[i] + 1] = cy[i] * cw[i];
+                srow[2 * 17 + pos[i] + 1] = cz[i] * cw[i];
+                srow[3 * 17 + pos[i] + 1] = cw[i];
             }
         }
     } else {
@@ -232,7 +246,7 @@ __device__ __forceinline__ float output_block4(const WarpCtx &w, const float *ro
                                                uint32_t &c0, uint32_t &c1, uint32_t &idx) {
     uint32_t a = to565(v0, *w.T), b = to565(v1, *w.T);
     if (a < b) { const uint32_t t = a; a = b; b = t; }
-    const PalF pal = palette_f(a, b, p.decoder, w.T->lut255);
+    const PalF pal = palette_f(a, b, p.decoder, w.T->lut255, w.D);
     c0 = a;
     c1 = b;
     return select_indices<4>(row, p.cw, pal, false, idx);
@@ -243,7 +257,7 @@ __device__ __forceinline__ float output_block3(const WarpCtx &w, const float *ro
                                                uint32_t &c0, uint32_t &c1, uint32_t &idx) {
     uint32_t a = to565(v0, *w.T), b = to565(v1, *w.T);
     if (a > b) { const uint32_t t = a; a = b; b = t; }
-    const PalF pal = palette_f(a, b, p.decoder, w.T->lut255);
+    const PalF pal = palette_f(a, b, p.decoder, w.T->lut255, w.D);
     c0 = a;
     c1 = b;
     return select_indices<3>(row, p.cw, pal, p.three_color_black != 0, idx);
@@ -254,7 +268,7 @@ __device__ __forceinline__ float output_block3(const WarpCtx &w, const float *ro
 __device__ __forceinline__ bool optimize_end_points4(const float *row, uint32_t indices, V3 &a, V3 &b) {
     float alpha2 = 0.0f, beta2 = 0.0f, ab = 0.0f;
     V3 ax = v3(0.0f, 0.0f, 0.0f), bx = v3(0.0f, 0.0f, 0.0f);
-#pragma unroll 4
+#pragma unroll 1
     for (int i = 0; i < 16; i++) {
         const uint32_t bits = indices >> (2 * i);
         float beta = (float)(bits & 1);
@@ -328,7 +342,7 @@ __device__ __forceinline__ uint32_t add565(uint32_t c, int dr, int dg, int db) {
 __device__ __forceinline__ uint32_t indices_generic(const float *row, V3 cw, const PalF &pal) {
     const V3 p0 = pal.c[0] * cw, p1 = pal.c[1] * cw, p2 = pal.c[2] * cw, p3 = pal.c[3] * cw;
     uint32_t out = 0;
-#pragma unroll 4
+#pragma unroll 1
     for (int t = 0; t < 16; t++) {
         const V3 c = texel(row, t) * cw;
         const V3 t0 = c - p0, t1 = c - p1, t2 = c - p2, t3 = c - p3;
@@ -348,7 +362,7 @@ __device__ __forceinline__ float refine(const WarpCtx &w, const float *row, cons
                                         uint32_t &c0, uint32_t &c1, uint32_t &idx) {
     float best = input_error;
     int last = 0;
-    uint32_t base_idx = indices_generic(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255));
+    uint32_t base_idx = indices_generic(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D));
     for (int i = 0; i < 256; i++) {
         const int d = i & 15;
         const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
@@ -359,7 +373,7 @@ __device__ __forceinline__ float refine(const WarpCtx &w, const float *row, cons
             if (r0 == r1) r1 = add565(r1, 0, 1, 0);
             if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
         }
-        const PalF pr = palette_f(r0, r1, p.decoder, w.T->lut255);
+        const PalF pr = palette_f(r0, r1, p.decoder, w.T->lut255, w.D);
         const float e = block_error(row, p.cw, pr, base_idx);
         if (e < best) {
             best = e;
@@ -376,25 +390,35 @@ __device__ __forceinline__ float refine(const WarpCtx &w, const float *row, cons
 
 // ---------------------------------------------------------- cluster fit --
 
-struct FitConst {
+// Per-block sums of a SAT (its last entry) and the warp-uniform weights.
+struct FitSums {
     float r_sum, g_sum, b_sum, w_sum;
+};
+
+struct FitWeights {
     float w1_3, w2_3, w1_9, w4_9, w2_9;
     V3 metric;
 };
 
-__device__ __forceinline__ FitConst fit_const(const float *S, int count, const DecoderTables *D, V3 metric) {
-    FitConst k;
+__device__ __forceinline__ FitSums fit_sums(const float *S, int count) {
+    FitSums k;
     k.r_sum = S[0 * 17 + count];
     k.g_sum = S[1 * 17 + count];
     k.b_sum = S[2 * 17 + count];
     k.w_sum = S[3 * 17 + count];
+    return k;
+}
+
+__device__ __forceinline__ FitWeights fit_weights(const DecoderTables *D, V3 metric) {
+    FitWeights k;
     k.w1_3 = D->w1_3; k.w2_3 = D->w2_3; k.w1_9 = D->w1_9; k.w4_9 = D->w4_9; k.w2_9 = D->w2_9;
     k.metric = metric;
     return k;
 }
 
 // One cluster_fit_four iteration (icbc.h:2650-2722), scalar arithmetic order.
-__device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, const FitConst &k, V3 &a, V3 &b) {
+__device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
+                                          V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
     V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
     V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
@@ -406,12 +430,12 @@ __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, cons
     x1 = x1 - x0;
     w2 = w2 - w1;
     w1 = w1 - w0;
-    const float alpha2 = w2 * k.w1_9 + (w1 * k.w4_9 + w0);
-    const float beta2 = w1 * k.w1_9 + (w2 * k.w4_9 + w3);
-    const float ab = (w1 + w2) * k.w2_9;
+    const float alpha2 = w2 * q.w1_9 + (w1 * q.w4_9 + w0);
+    const float beta2 = w1 * q.w1_9 + (w2 * q.w4_9 + w3);
+    const float ab = (w1 + w2) * q.w2_9;
     const float factor = 1.0f / (alpha2 * beta2 - ab * ab);
-    const V3 ax = v3(x2.x * k.w1_3 + (x1.x * k.w2_3 + x0.x), x2.y * k.w1_3 + (x1.y * k.w2_3 + x0.y),
-                     x2.z * k.w1_3 + (x1.z * k.w2_3 + x0.z));
+    const V3 ax = v3(x2.x * q.w1_3 + (x1.x * q.w2_3 + x0.x), x2.y * q.w1_3 + (x1.y * q.w2_3 + x0.y),
+                     x2.z * q.w1_3 + (x1.z * q.w2_3 + x0.z));
     const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
     a = round_ept(v3((ax.x * beta2 - bx.x * ab) * factor, (ax.y * beta2 - bx.y * ab) * factor,
                      (ax.z * beta2 - bx.z * ab) * factor));
@@ -422,11 +446,12 @@ __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, cons
     const V3 e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + e2.x),
                      (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + e2.y),
                      (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + e2.z));
-    return dot(e1, k.metric);
+    return dot(e1, q.metric);
 }
 
 // One cluster_fit_three iteration (icbc.h:2273-2323).
-__device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, const FitConst &k, V3 &a, V3 &b) {
+__device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
+                                          V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
     const V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
     V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
@@ -450,34 +475,137 @@ __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, cons
     const V3 e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + e2.x),
                      (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + e2.y),
                      (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + e2.z));
-    return dot(e1, k.metric);
+    return dot(e1, q.metric);
 }
 
-// Warp-cooperative search of one block's combinations.  Returns the table
-// index of the first strict minimum, or -1 when no error is below FLT_MAX
-// (the reference then keeps zero endpoints).
+// Warp-cooperative search of the cluster combinations of every block of the
+// warp that needs one.  The warp's whole work -- the concatenation of each
+// block's combination list -- is cut into 64 equal contiguous ranges; lane l
+// walks ranges l and l + 32 side by side (two independent dependency
+// chains).  A walker keeps the first strict minimum of its share of a block
+// and, when it leaves the block, folds (error, table index) into the block's
+// slot with a 64-bit atomicMin on an order-preserving key.  The minimum key
+// is the smallest error with ties to the lowest table index: the combination
+// the sequential loop of icbc.h:2089-2344 / :2362-2742 keeps.  Errors equal
+// to zero are keyed as +0 because the loop's strict < treats -0 and +0 alike.
+struct Walker {
+    int g, gend;      // global combination range still to do
+    int b, k, total;  // current block, its combination index, its count
+    const float *S;
+    FitSums sums;
+    float best;
+    int best_k;
+};
+
+__device__ __forceinline__ int block_info(const WarpCtx &w, int b) { return __float_as_int(w.sat[b * kSatStride + 68]); }
+
 template <bool FOUR>
-__device__ __forceinline__ int coop_search(const WarpCtx &w, const float *S, int count, const FitConst &k) {
-    const int total = FOUR ? w.T->four_total[count - 1] : w.T->three_total[count - 1];
-    float best = FLT_MAX;
-    int best_i = 0x7fffffff;
-    // Two combinations per lane per iteration (independent dependency chains).
-    // Past the end the second one repeats the first, which a strict < never keeps.
-    for (int i = w.lane; i < total; i += 64) {
-        const int j = i + 32 < total ? i + 32 : i;
-        V3 a, b;
-        const float ei = FOUR ? cf4_combo(S, w.T->four[i], k, a, b) : cf3_combo(S, w.T->three[i], k, a, b);
-        const float ej = FOUR ? cf4_combo(S, w.T->four[j], k, a, b) : cf3_combo(S, w.T->three[j], k, a, b);
-        if (ei < best) { best = ei; best_i = i; }
-        if (ej < best) { best = ej; best_i = j; }
+__device__ __forceinline__ void walker_enter(const WarpCtx &w, Walker &v, int b, int k) {
+    const float *S = w.sat + b * kSatStride;
+    const int cnt = __float_as_int(S[68]) >> 16;
+    v.b = b;
+    v.k = k;
+    v.S = S;
+    v.total = FOUR ? w.T->four_total[cnt - 1] : w.T->three_total[cnt - 1];
+    v.sums = fit_sums(S, cnt);
+    v.best = FLT_MAX;
+    v.best_k = 0x7fffffff;
+}
+
+__device__ __forceinline__ void walker_flush(const WarpCtx &w, const Walker &v) {
+    if (v.best_k != 0x7fffffff) {
+        const float f = v.best == 0.0f ? 0.0f : v.best;
+        uint32_t u = __float_as_uint(f);
+        u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        atomicMin(&w.slots[v.b], ((unsigned long long)u << 32) | (uint32_t)v.best_k);
     }
+}
+
+// Starts a walker at global combination g (if any work is left for it).
+template <bool FOUR>
+__device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g, int gend) {
+    v.g = g;
+    v.gend = gend;
+    v.S = w.sat;
+    v.k = 0;
+    v.total = 1;
+    v.sums = FitSums{0.0f, 0.0f, 0.0f, 0.0f};
+    v.best = FLT_MAX;
+    v.best_k = 0x7fffffff;
+    v.b = 0;
+    if (g < gend) {
+        // The last block whose first combination is <= g always has work.
+        int lo = 0, hi = 32;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if ((block_info(w, mid) & 0xffff) <= g) lo = mid;
+            else hi = mid;
+        }
+        walker_enter<FOUR>(w, v, lo, g - (block_info(w, lo) & 0xffff));
+    }
+}
+
+// One step: fold the error of combination k in, move to k + 1, and cross
+// into the next block with work when this one is done.  `next` is the table
+// entry of the following combination, loaded one iteration ahead; a block
+// change reloads it.
+template <bool FOUR>
+__device__ __forceinline__ void walker_step(const WarpCtx &w, Walker &v, float e, uint32_t &next) {
+    const bool live = v.g < v.gend;
+    const bool better = live && e < v.best;
+    v.best = better ? e : v.best;
+    v.best_k = better ? v.k : v.best_k;
+    v.g += live;
+    v.k += live;
+    if (live && v.k == v.total && v.g < v.gend) {
+        walker_flush(w, v);
+        int nb = v.b + 1;
+        while ((block_info(w, nb) >> 16) == 0) nb++;
+        walker_enter<FOUR>(w, v, nb, 0);
+        next = (FOUR ? w.T->four : w.T->three)[0];
+    }
+}
+
+// Returns this lane's winning table index, or -1 (no search, or no error
+// below FLT_MAX: the reference then keeps zero endpoints).
+template <bool FOUR>
+__device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int count, const FitWeights &q) {
+    const int lane = w.lane;
+    const int T = need ? (FOUR ? w.T->four_total[count - 1] : w.T->three_total[count - 1]) : 0;
+    int incl = T;
 #pragma unroll
-    for (int off = 16; off; off >>= 1) {
-        const float ob = __shfl_xor_sync(kFull, best, off);
-        const int oi = __shfl_xor_sync(kFull, best_i, off);
-        if (ob < best || (ob == best && oi < best_i)) { best = ob; best_i = oi; }
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += y;
     }
-    return best_i == 0x7fffffff ? -1 : best_i;
+    const int W = __shfl_sync(kFull, incl, 31);
+    w.sat[lane * kSatStride + 68] = __int_as_float((incl - T) | ((need ? count : 0) << 16));
+    w.slots[lane] = ~0ull;
+    __syncwarp();
+    if (W == 0) return -1;
+    const int per = (W + 63) / 64;
+    Walker A, B;
+    walker_start<FOUR>(w, A, min(lane * per, W), min(lane * per + per, W));
+    walker_start<FOUR>(w, B, min((lane + 32) * per, W), min((lane + 32) * per + per, W));
+    const uint32_t *table = FOUR ? w.T->four : w.T->three;
+    uint32_t pa = table[A.k], pb = table[B.k];
+    for (int it = 0; it < per; it++) {
+        // Entry k + 1 of each walker is fetched before this step's arithmetic
+        // (the tables are padded past their last used entry).
+        uint32_t na = table[A.k + 1], nb = table[B.k + 1];
+        V3 a, b;
+        const float ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
+        const float eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
+        walker_step<FOUR>(w, A, ea, na);
+        walker_step<FOUR>(w, B, eb, nb);
+        pa = na;
+        pb = nb;
+    }
+    walker_flush(w, A);
+    walker_flush(w, B);
+    __syncwarp();
+    const unsigned long long key = w.slots[lane];
+    return (need && key != ~0ull) ? (int)(uint32_t)key : -1;
 }
 
 // ------------------------------------------------------------- encoder --
@@ -504,7 +632,7 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
             err = 0.0f;
         } else if (O::cluster && count == 1) {
             single_color(w.D, texel(srow, 0), c0, c1, idx);
-            err = block_error(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255), idx);
+            err = block_error(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D), idx);
         } else {
             live = true;
             err = FLT_MAX;
@@ -528,23 +656,16 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
     if (O::cluster) {
         const V3 metric = p.cw * p.cw;
         __syncwarp();
-        // 4-colour cluster fit, one block at a time across the warp.
-        int my4 = -1;
-        for (unsigned mask = __ballot_sync(kFull, need4); mask; mask &= mask - 1) {
-            const int bb = __ffs(mask) - 1;
-            const int cnt = __shfl_sync(kFull, count, bb);
-            const float *S = w.sat + bb * kSatStride;
-            const int k = coop_search<true>(w, S, cnt, fit_const(S, cnt, w.D, metric));
-            if (lane == bb) my4 = k;
-        }
-        __syncwarp();
+        // 4-colour cluster fit of every block that needs one, across the warp.
+        const FitWeights q = fit_weights(w.D, metric);
+        const int my4 = flat_search<true>(w, need4, count, q);
         uint32_t f0 = 0, f1 = 0, fi = 0;
         float ferr = 0.0f;
         bool need3 = false;
         int count3 = count;
         if (need4) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
-            if (my4 >= 0) cf4_combo(srow, w.T->four[my4], fit_const(srow, count, w.D, metric), a, b);
+            if (my4 >= 0) cf4_combo(srow, w.T->four[my4], fit_sums(srow, count), q, a, b);
             ferr = output_block4(w, row, p, a, b, f0, f1, fi);
             const bool use_black = any_black && p.three_color_black;
             const bool use_three = (O::cf3_always && p.three_color_mode) ||
@@ -563,17 +684,10 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
             }
         }
         __syncwarp();
-        int my3 = -1;
-        for (unsigned mask = __ballot_sync(kFull, need3); mask; mask &= mask - 1) {
-            const int bb = __ffs(mask) - 1;
-            const int cnt = __shfl_sync(kFull, count3, bb);
-            const float *S = w.sat + bb * kSatStride;
-            const int k = coop_search<false>(w, S, cnt, fit_const(S, cnt, w.D, metric));
-            if (lane == bb) my3 = k;
-        }
+        const int my3 = flat_search<false>(w, need3, count3, q);
         if (need3) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
-            if (my3 >= 0) cf3_combo(srow, w.T->three[my3], fit_const(srow, count3, w.D, metric), a, b);
+            if (my3 >= 0) cf3_combo(srow, w.T->three[my3], fit_sums(srow, count3), q, a, b);
             uint32_t t0, t1, ti;
             const float e3 = output_block3(w, row, p, a, b, t0, t1, ti);
             if (e3 < ferr) { ferr = e3; f0 = t0; f1 = t1; fi = ti; }

@@ -114,6 +114,14 @@ void build_tables(GlobalTables &G) {
         D.w2_9 = w1_3 * w2_3;
         build_match(D.match5, 5, d);
         build_match(D.match6, 6, d);
+        // Linear palette forms (entries 2/3 of icbc.h:2752-2874), NVIDIA unused.
+        static const int kLin[4][8] = {
+            {87382, 43691, 0, 17, 1, 1, 0, 1},   // D3D10: (2a+b)/3 exact for a, b <= 255; (a+b)/2
+            {0, 0, 0, 0, 0, 0, 0, 0},            // NVIDIA: own formulas
+            {43, 21, 32, 6, 1, 1, 1, 1},         // AMD: (43a+21b+32)>>6; (a+b+1)/2
+            {171, 85, 128, 8, 128, 128, 128, 8}  // Intel: (171a+85b+128)>>8; (128a+128b+128)>>8
+        };
+        std::memcpy(D.lin, kLin[d], sizeof(D.lin));
     }
 }
 
