@@ -273,6 +273,9 @@ def run_ours(args):
     if rank != 0:
         return
     batch = None if (args.no_batch or args.no_cpu_baseline) else batch_leg(ig, torch, dev, args)
+    serving = None
+    if not (args.no_serve or args.no_cpu_baseline):
+        serving = serving_leg(ig, args, batch["batched"]["gpix_s"] if batch else None)
     if args.no_cpu_baseline:
         print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                           "warmup": args.warmup, "ms_per_step": step_ms, "levels": LEVELS,
@@ -324,6 +327,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step"},
         "batch": batch,
+        "serving": serving,
         "gpu_launches": args.steps * len(LEVELS),
         "clocks": clk,
         "wall_s_timed": wall,
@@ -414,6 +418,49 @@ def batch_leg(ig, torch, dev, args):
             "launches_plain": len(specs), "launches_batched": 1}
 
 
+def serving_leg(ig, args, batched_gpix):
+    """Serving workload: Poisson arrivals, sides {64..2048} with probabilities
+    {.30,.25,.20,.15,.07,.03}, level uniform 0..9, D3D10, 40 GB HBM budget.
+    Latency is submit -> blocks in the caller's host buffer."""
+    from icbc_gb300 import synth
+    bases = [synth.gradient_noise_rects(2048, 2048, 300 + k) for k in range(2)]
+    pool = {}
+    for side in synth.SERVING_SIDES:
+        crops = []
+        for k in range(3):
+            y0, x0 = (k * 389) % (2049 - side), (k * 211) % (2049 - side)
+            crops.append(np.ascontiguousarray(bases[k % 2][y0:y0 + side, x0:x0 + side]))
+        pool[side] = crops
+    runs = []
+    for rate in args.serve_rates:
+        n = int(min(args.serve_max_requests, max(400, rate * args.serve_seconds)))
+        reqs = synth.serving_requests(n, rate, seed=int(rate))
+        outs = [np.empty((ig.blocks_of(r.side, r.side), 8), np.uint8) for r in reqs]
+        srv = ig.Server(40 << 30, max_inflight=3, max_batch_images=1024)
+        ids = []
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            while True:
+                dt = r.arrival_s - (time.perf_counter() - t0)
+                if dt <= 0:
+                    break
+                if dt > 2e-3:
+                    time.sleep(dt - 1e-3)
+            ids.append(srv.submit(pool[r.side][i % 3], r.level, ig.Decoder_D3D10, out=outs[i]))
+        for rid in ids:
+            srv.wait(rid, 120000)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        px = sum(r.side * r.side for r in reqs)
+        runs.append({"rate_req_s": rate, "requests": n, "offered_gpix_s": px / reqs[-1].arrival_s / 1e9,
+                     "gpix_s": st["pixels_completed"] / wall / 1e9, "p50_ms": st["latency_p50_ms"],
+                     "p99_ms": st["latency_p99_ms"], "mean_ms": st["latency_mean_ms"], "max_ms": st["latency_max_ms"],
+                     "batches": st["batches"], "arena_peak_bytes": st["arena_peak"], "completed": st["completed"]})
+    return {"workload": "poisson_serving", "hbm_budget_bytes": 40 << 30, "max_inflight": 3,
+            "batched_offline_gpix_s": batched_gpix, "runs": runs}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,6 +476,10 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
     ap.add_argument("--batch-images", type=int, default=2000)
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 5000, 20000])
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-max-requests", type=int, default=4000)
     args = ap.parse_args()
     if args.levels:
         global LEVELS

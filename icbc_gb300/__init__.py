@@ -48,6 +48,33 @@ class ImageDesc(ctypes.Structure):
                 ("color_weights", ctypes.c_float * 3), ("out", ctypes.c_void_p), ("errors", ctypes.c_void_p)]
 
 
+class ServerConfig(ctypes.Structure):
+    """struct icbc_gpu_server_config."""
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_inflight", ctypes.c_int32),
+                ("max_batch_images", ctypes.c_int32)]
+
+
+class RequestDesc(ctypes.Structure):
+    """struct icbc_gpu_request."""
+    _fields_ = [("rgba", ctypes.c_void_p), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("pitch", ctypes.c_int64), ("weight_mode", ctypes.c_int32), ("level", ctypes.c_int32),
+                ("decoder", ctypes.c_int32), ("three_color_mode", ctypes.c_int32),
+                ("three_color_black", ctypes.c_int32), ("color_weights", ctypes.c_float * 3),
+                ("out", ctypes.c_void_p), ("errors", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    """struct icbc_gpu_server_stats."""
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "rejected", "cancelled", "failed",
+                                              "pending", "in_flight", "batches", "arena_bytes", "arena_used",
+                                              "arena_peak")] + \
+               [(n, ctypes.c_double) for n in ("pixels_completed", "latency_mean_ms", "latency_p50_ms",
+                                               "latency_p99_ms", "latency_max_ms")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -86,6 +113,13 @@ def load(build_if_missing: bool = True):
             "icbc_gpu_evaluate_bc1_error": (i32, [vp, vp, vp, i64, i32, vp]),
             "icbc_gpu_compress_bc1_image_host": (i32, [vp, i32, i32, i64, i32, vp, i32, i32, i32, i32, f32p, vp, vp]),
             "icbc_gpu_debug_tables": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
+            "icbc_gpu_server_create": (i32, [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),
+            "icbc_gpu_server_submit": (i32, [vp, ctypes.POINTER(RequestDesc), ctypes.POINTER(ctypes.c_uint64)]),
+            "icbc_gpu_server_poll": (i32, [vp, ctypes.c_uint64]),
+            "icbc_gpu_server_wait": (i32, [vp, ctypes.c_uint64, ctypes.c_int32]),
+            "icbc_gpu_server_cancel": (i32, [vp, ctypes.c_uint64]),
+            "icbc_gpu_server_get_stats": (i32, [vp, ctypes.POINTER(ServerStats)]),
+            "icbc_gpu_server_destroy": (i32, [vp]),
             "icbc_gpu_compress_bc1_images_noalloc": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
         }
         for name, (res, args) in sig.items():
@@ -348,3 +382,67 @@ def compress_image_host(rgba: np.ndarray, level: int, decoder: int = DECODER_DEF
                                             _cw(color_weights), optr, eptr)
     _check(st, "compress_bc1_image_host")
     return out
+
+
+class Server:
+    """The serving form (icbc_gpu_server_*): submit host RGBA8 images as they
+    arrive; they are admitted under the HBM budget and batched onto the GPU.
+    Host arrays are kept alive here until their request finishes."""
+
+    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 2, max_batch_images: int = 512):
+        L = load()
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_inflight), int(max_batch_images))
+        h = ctypes.c_void_p()
+        _check(L.icbc_gpu_server_create(ctypes.byref(cfg), ctypes.byref(h)), "server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit(self, rgba: np.ndarray, level: int, decoder: int = Decoder_D3D10, color_weights=(1.0, 1.0, 1.0),
+               weight_mode: int = WEIGHTS_UNIFORM, three_color_mode: bool = True, three_color_black: bool = True,
+               out: np.ndarray | None = None, errors: np.ndarray | None = None) -> int:
+        """Queues one image; returns the request id.  Raises IcbcGpuError
+        (status ICBC_GPU_ERR_BUDGET etc.) when the request is refused."""
+        h, w = int(rgba.shape[0]), int(rgba.shape[1])
+        if out is None:
+            out = np.zeros((blocks_of(w, h), 8), np.uint8)
+        r = RequestDesc()
+        r.rgba = rgba.ctypes.data
+        r.width, r.height, r.pitch = w, h, int(rgba.strides[0])
+        r.weight_mode, r.level, r.decoder = int(weight_mode), int(level), int(decoder)
+        r.three_color_mode, r.three_color_black = int(bool(three_color_mode)), int(bool(three_color_black))
+        r.color_weights = (ctypes.c_float * 3)(*[float(x) for x in color_weights])
+        r.out = out.ctypes.data
+        r.errors = errors.ctypes.data if errors is not None else None
+        rid = ctypes.c_uint64()
+        _check(load().icbc_gpu_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)), "server_submit")
+        self._keep[rid.value] = (rgba, out, errors)
+        return rid.value
+
+    def result(self, rid: int):
+        """(blocks, errors) of a finished request."""
+        return self._keep[rid][1], self._keep[rid][2]
+
+    def poll(self, rid: int) -> int:
+        return load().icbc_gpu_server_poll(self._h, int(rid))
+
+    def wait(self, rid: int, timeout_ms: int = -1) -> int:
+        return load().icbc_gpu_server_wait(self._h, int(rid), int(timeout_ms))
+
+    def cancel(self, rid: int) -> int:
+        return load().icbc_gpu_server_cancel(self._h, int(rid))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(load().icbc_gpu_server_get_stats(self._h, ctypes.byref(st)), "server_get_stats")
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            load().icbc_gpu_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -8,9 +8,13 @@ namespace icbc_gpu {
 
 // Persistent batched encoder: every warp takes the next task (32 blocks of
 // one image) from an atomic counter until the queue is empty.  Tasks are
-// ordered most expensive level first by the planner.
+// ordered most expensive level first by the planner.  A task is either an
+// entry of an explicit list (`tasks`), or -- when `tasks` is NULL -- found from
+// per-image offsets: task t belongs to the last image whose first task
+// (`task_start[i]`, n_images + 1 entries) is <= t.
 __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const GlobalTables *G, const ImageDesc *images,
-                                                                     const BatchTask *tasks, int ntasks, int *counter) {
+                                                                     const BatchTask *tasks, const uint32_t *task_start,
+                                                                     int n_images, int ntasks, int *counter) {
     extern __shared__ __align__(16) unsigned char smem[];
     SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
     stage_tables(T, G);
@@ -20,7 +24,19 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
         if (lane == 0) t = atomicAdd(counter, 1);
         t = __shfl_sync(kFull, t, 0);
         if (t >= ntasks) break;
-        const BatchTask task = tasks[t];
+        BatchTask task;
+        if (tasks) {
+            task = tasks[t];
+        } else {
+            int lo = 0, hi = n_images;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if ((int)task_start[mid] <= t) lo = mid;
+                else hi = mid;
+            }
+            task.image = (uint32_t)lo;
+            task.first_block = (uint32_t)(t - (int)task_start[lo]) * 32u;
+        }
         const ImageDesc &d = images[task.image];
         const int level = d.level;
         const int64_t b = (int64_t)task.first_block + lane;
@@ -61,12 +77,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
     }
 }
 
-cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
-                                int *counter, cudaStream_t stream, int grid) {
+cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                const uint32_t *task_start, int n_images, int ntasks, int *counter,
+                                cudaStream_t stream, int grid) {
     const size_t smem = smem_bytes(true);
     cudaError_t e = cudaFuncSetAttribute(k_encode_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_encode_batch<<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, ntasks, counter);
+    k_encode_batch<<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, task_start, n_images, ntasks, counter);
     return cudaGetLastError();
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/icbc_gpu.h"
 #include "bc1_encode.cuh"
 
 namespace icbc_gpu {
@@ -57,8 +58,9 @@ ICBC_DECLARE_LEVEL(8)
 ICBC_DECLARE_LEVEL(9)
 #undef ICBC_DECLARE_LEVEL
 
-cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
-                                int *counter, cudaStream_t stream, int grid);
+cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                const uint32_t *task_start, int n_images, int ntasks, int *counter,
+                                cudaStream_t stream, int grid);
 int batch_ctas_per_sm();
 cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder, cudaStream_t stream);
 cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
@@ -66,6 +68,8 @@ cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors,
 
 // Host-side services of icbc_gpu_api.cu used by other translation units.
 const GlobalTables &host_tables();
+int ensure_tables_on_device(const GlobalTables **out);
+int resolve_image_desc_checked(const icbc_gpu_image &image, ImageDesc &desc);
 int level_cost(int level);
 int current_sm_count();
 

@@ -242,6 +242,10 @@ const GlobalTables &host_tables() {
 
 int resolve_image_desc(const icbc_gpu_image &image, ImageDesc &desc) { return resolve_image(image, desc); }
 
+int resolve_image_desc_checked(const icbc_gpu_image &image, ImageDesc &desc) { return resolve_image(image, desc); }
+
+int ensure_tables_on_device(const GlobalTables **out) { return ensure_device_tables(out); }
+
 int current_sm_count() { return sm_count(); }
 
 }  // namespace icbc_gpu
@@ -403,7 +407,7 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     if (e == cudaSuccess) {
         cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int), cs);
         cudaError_t e2 = e1 == cudaSuccess && B->ntasks
-                             ? launch_encode_batch(G, B->d_images, B->d_tasks, B->ntasks, B->d_counter, cs, B->grid)
+                             ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter, cs, B->grid)
                              : e1;
         e = cudaStreamEndCapture(cs, &B->graph);
         if (e1 != cudaSuccess) e = e1;

@@ -182,6 +182,65 @@ int icbc_gpu_compress_bc1_image_host(const uint8_t *rgba, int32_t width, int32_t
                                      int32_t decoder, int32_t three_color_mode, int32_t three_color_black,
                                      const float color_weights[3], void *out, float *errors);
 
+/* ------------------------------------------------------------------------
+ * Serving form (no counterpart in the reference, which encodes on the
+ * caller's thread): a request loop that batches encode requests of any size
+ * and level as they arrive.  Texels and blocks are staged in one device arena
+ * of hbm_budget_bytes allocated at create; a request is admitted (FIFO) once
+ * its bytes fit in the arena, so requests that arrive while others run join
+ * the next batched launch as memory frees up, and up to max_inflight batches
+ * run on the GPU at once.  Results equal the single-image encode bit for bit.
+ * ---------------------------------------------------------------------- */
+typedef struct icbc_gpu_server icbc_gpu_server;
+
+typedef struct icbc_gpu_server_config {
+    int64_t hbm_budget_bytes;   /* device arena for staged texels and blocks (> 0) */
+    int32_t max_inflight;       /* batched launches on the GPU at once (1..8) */
+    int32_t max_batch_images;   /* images per batched launch (1..4096) */
+} icbc_gpu_server_config;
+
+/* One encode request.  Host buffers stay owned by the caller and must stay
+ * valid until the request completes or is cancelled. */
+typedef struct icbc_gpu_request {
+    const uint8_t *rgba;        /* host RGBA8 rows */
+    int32_t width, height;
+    int64_t pitch;              /* bytes between rows */
+    int32_t weight_mode;        /* ICBC_GPU_WEIGHTS_UNIFORM or _ALPHA */
+    int32_t level, decoder, three_color_mode, three_color_black;
+    float color_weights[3];
+    void *out;                  /* host, ceil(w/4) * ceil(h/4) * 8 bytes, written on completion */
+    float *errors;              /* host, one float per block, or NULL */
+} icbc_gpu_request;
+
+typedef struct icbc_gpu_server_stats {
+    int64_t submitted, completed, rejected, cancelled, failed;
+    int64_t pending, in_flight, batches;
+    int64_t arena_bytes, arena_used, arena_peak;
+    double pixels_completed;
+    double latency_mean_ms, latency_p50_ms, latency_p99_ms, latency_max_ms;  /* submit -> blocks on host */
+} icbc_gpu_server_stats;
+
+/* Creates the server on the current device: allocates the arena and pinned
+ * staging, starts the scheduler thread. */
+int icbc_gpu_server_create(const icbc_gpu_server_config *config, icbc_gpu_server **server);
+/* Queues a request; returns its id.  The texels are copied to pinned staging
+ * on the calling thread when there is room (else at launch, from `rgba`).
+ * ICBC_GPU_ERR_BUDGET if it can never fit in the arena,
+ * ICBC_GPU_ERR_INVALID_ARGUMENT for a malformed request.  Thread-safe. */
+int icbc_gpu_server_submit(icbc_gpu_server *server, const icbc_gpu_request *request, uint64_t *id);
+/* ICBC_GPU_OK when done, ICBC_GPU_ERR_NOT_READY while queued or running,
+ * ICBC_GPU_ERR_CANCELLED, ICBC_GPU_ERR_NOT_FOUND, or the failure status. */
+int icbc_gpu_server_poll(icbc_gpu_server *server, uint64_t id);
+/* As poll, blocking up to timeout_ms (< 0: no limit). */
+int icbc_gpu_server_wait(icbc_gpu_server *server, uint64_t id, int32_t timeout_ms);
+/* Cancels a request that has not been admitted yet (ICBC_GPU_ERR_NOT_READY if
+ * it is already on the GPU). */
+int icbc_gpu_server_cancel(icbc_gpu_server *server, uint64_t id);
+int icbc_gpu_server_get_stats(icbc_gpu_server *server, icbc_gpu_server_stats *stats);
+/* Stops the scheduler; pending requests are cancelled, running ones finish.
+ * Must not run concurrently with other calls on the same server. */
+int icbc_gpu_server_destroy(icbc_gpu_server *server);
+
 /* Number of SMs of the current device (for sizing host-side work). */
 int icbc_gpu_sm_count(void);
 
