@@ -297,6 +297,7 @@ def run_ours(args):
     ops = {lv: algorithmic_ops(cstats[lv], lv) * scale for lv in LEVELS}
     peaks = load_peaks()
     peak = fp32_peak_tops(peaks, sms)
+    hard = None if args.no_hard else hard_leg(ig, torch, dev, args, peak)
     top = max(LEVELS, key=lambda lv: lvl_ms[lv])
     achieved = ops[top] / (lvl_ms[top] * 1e-3) / 1e12
     per_level = {str(lv): {"gpix_s": px / (lvl_ms[lv] * 1e-3) / 1e9, "ms": lvl_ms[lv],
@@ -328,6 +329,7 @@ def run_ours(args):
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step"},
         "batch": batch,
         "serving": serving,
+        "hard": hard,
         "gpu_launches": args.steps * len(LEVELS),
         "clocks": clk,
         "wall_s_timed": wall,
@@ -436,17 +438,30 @@ def serving_leg(ig, args, batched_gpix):
         n = int(min(args.serve_max_requests, max(400, rate * args.serve_seconds)))
         reqs = synth.serving_requests(n, rate, seed=int(rate))
         outs = [np.empty((ig.blocks_of(r.side, r.side), 8), np.uint8) for r in reqs]
-        srv = ig.Server(40 << 30, max_inflight=3, max_batch_images=1024)
-        ids = []
+        srv = ig.Server(40 << 30, max_inflight=4, max_batch_images=1024)
+        ids = [None] * n
+        nthreads = args.serve_threads
+
+        def submitter(k, t0):
+            # Thread k submits requests k, k + nthreads, ... at their arrival
+            # times (ctypes releases the GIL inside the call).
+            for i in range(k, n, nthreads):
+                r = reqs[i]
+                while True:
+                    dt = r.arrival_s - (time.perf_counter() - t0)
+                    if dt <= 0:
+                        break
+                    if dt > 2e-3:
+                        time.sleep(dt - 1e-3)
+                ids[i] = srv.submit(pool[r.side][i % 3], r.level, ig.Decoder_D3D10, out=outs[i])
+
         t0 = time.perf_counter()
-        for i, r in enumerate(reqs):
-            while True:
-                dt = r.arrival_s - (time.perf_counter() - t0)
-                if dt <= 0:
-                    break
-                if dt > 2e-3:
-                    time.sleep(dt - 1e-3)
-            ids.append(srv.submit(pool[r.side][i % 3], r.level, ig.Decoder_D3D10, out=outs[i]))
+        threads = [threading.Thread(target=submitter, args=(k, t0)) for k in range(nthreads)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        submit_span = time.perf_counter() - t0
         for rid in ids:
             srv.wait(rid, 120000)
         wall = time.perf_counter() - t0
@@ -454,11 +469,85 @@ def serving_leg(ig, args, batched_gpix):
         srv.close()
         px = sum(r.side * r.side for r in reqs)
         runs.append({"rate_req_s": rate, "requests": n, "offered_gpix_s": px / reqs[-1].arrival_s / 1e9,
+                     "achieved_submit_rate_req_s": n / submit_span, "submit_threads": nthreads,
                      "gpix_s": st["pixels_completed"] / wall / 1e9, "p50_ms": st["latency_p50_ms"],
                      "p99_ms": st["latency_p99_ms"], "mean_ms": st["latency_mean_ms"], "max_ms": st["latency_max_ms"],
                      "batches": st["batches"], "arena_peak_bytes": st["arena_peak"], "completed": st["completed"]})
-    return {"workload": "poisson_serving", "hbm_budget_bytes": 40 << 30, "max_inflight": 3,
+    return {"workload": "poisson_serving", "hbm_budget_bytes": 40 << 30, "max_inflight": 4,
             "batched_offline_gpix_s": batched_gpix, "runs": runs}
+
+
+def hard_leg(ig, torch, dev, args, peak_tops):
+    """Hard-distribution batch: args.hard_images images of args.hard_side^2
+    drawn from the block mixture (30% noise, 20% two-colour dither, 15% single
+    colour, 15% near-black, 20% gradient+noise; 25% zero-weight texels via
+    alpha), Quality_Max, both three-colour modes, weights = alpha/255.
+    Batched (one persistent launch) against plain (one launch per image);
+    sampled bit-exactness against the oracle, per-image RMSE/PSNR from an FP64
+    decode-and-compare, and the FP32 fraction."""
+    from icbc_gb300 import synth
+    from oracle import oracle as O
+    n, side = args.hard_images, args.hard_side
+    nb = ig.blocks_of(side, side)
+    imgs = [synth.hard_mixture_torch(side, side, 1000 + i, dev) for i in range(n)]
+    outs_b = [torch.zeros((nb, 8), dtype=torch.uint8, device=dev) for _ in range(n)]
+    outs_p = [torch.zeros((nb, 8), dtype=torch.uint8, device=dev) for _ in range(n)]
+    cw = (1.0, 1.0, 1.0)
+    descs_b = [ig.image_desc(im, 9, o, None, ig.Decoder_D3D10, cw, ig.WEIGHTS_ALPHA) for im, o in zip(imgs, outs_b)]
+    descs_p = [ig.image_desc(im, 9, o, None, ig.Decoder_D3D10, cw, ig.WEIGHTS_ALPHA) for im, o in zip(imgs, outs_p)]
+    stream = torch.cuda.Stream(device=dev)
+    batch = ig.Batch(descs_b)
+    res = {}
+    for name, fn in (("batched", lambda: batch.launch(stream)), ("plain", lambda: ig.compress_images_each(descs_p, stream))):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            fn()
+            e0.record(stream)
+            for _ in range(args.hard_steps):
+                fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.hard_steps
+        res[name] = {"ms": ms, "gpix_s": n * side * side / (ms * 1e-3) / 1e9}
+    batch.close()
+    same = all(torch.equal(a, b) for a, b in zip(outs_b, outs_p))
+    # sampled oracle parity + op counts: every 97th block row of every 8th image
+    mism, sampled, stats = 0, 0, None
+    for i in range(0, n, 8):
+        host = imgs[i].cpu().numpy()
+        rows = sample_rows(host, 97)
+        ob, _, st = O.encode_image(rows, 9, 0, cw, 1, None, True, True, nthreads=os.cpu_count() or 1,
+                                   with_stats=True)
+        gpu = outs_b[i].cpu().numpy().reshape(side // 4, side // 4, 8)[::97].reshape(-1, 8)
+        mism += int((gpu != ob).any(1).sum())
+        sampled += ob.shape[0]
+        stats = st if stats is None else {k: stats[k] + st[k] for k in st}
+    ops = algorithmic_ops(stats, 9) * (n * nb) / stats["blocks"]
+    # FP64 decode-and-compare on the GPU: exact per-block integer SSE, FP64 sums
+    psnr = []
+    sse_total = 0.0
+    for im, o in zip(imgs, outs_b):
+        tex = im.view(side // 4, 4, side // 4, 4, 4).permute(0, 2, 1, 3, 4).reshape(nb, 64).contiguous()
+        e = ig.evaluate_errors(tex, o, ig.Decoder_D3D10)
+        sse = float(e.double().sum())
+        sse_total += sse
+        mse = sse / (16 * nb)
+        psnr.append(20 * np.log10(255.0 / np.sqrt(mse)) if mse > 0 else 300.0)
+    # the GPU SSE equals the oracle's FP64 decode-and-compare on one image
+    sse0 = O.image_sse(imgs[0].cpu().numpy(), outs_b[0].cpu().numpy(), 0)
+    ev0 = float(ig.evaluate_errors(imgs[0].view(side // 4, 4, side // 4, 4, 4).permute(0, 2, 1, 3, 4)
+                                   .reshape(nb, 64).contiguous(), outs_b[0], 0).double().sum())
+    mse = sse_total / (16 * n * nb)
+    del imgs, outs_b, outs_p
+    torch.cuda.empty_cache()
+    return {"workload": "hard_mixture_%dx%d^2_L9" % (n, side), "blocks": n * nb,
+            "batched": res["batched"], "plain": res["plain"],
+            "speedup_batched_over_plain": res["plain"]["ms"] / res["batched"]["ms"],
+            "batched_equals_plain": bool(same), "oracle_sampled_blocks": sampled, "oracle_mismatches": mism,
+            "rmse": float(np.sqrt(mse)), "psnr_db": float(20 * np.log10(255.0 / np.sqrt(mse))),
+            "psnr_db_per_image_min_max": [float(min(psnr)), float(max(psnr))],
+            "fp64_sse_image0_gpu_vs_oracle": [ev0, sse0],
+            "fp32_frac": ops / (res["batched"]["ms"] * 1e-3) / 1e12 / peak_tops}
 
 
 def main():
@@ -477,9 +566,14 @@ def main():
     ap.add_argument("--batch-images", type=int, default=2000)
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-hard", action="store_true", help="skip the hard-distribution leg")
+    ap.add_argument("--hard-images", type=int, default=64)
+    ap.add_argument("--hard-side", type=int, default=8192)
+    ap.add_argument("--hard-steps", type=int, default=2)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 5000, 20000])
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-max-requests", type=int, default=4000)
+    ap.add_argument("--serve-threads", type=int, default=4)
     args = ap.parse_args()
     if args.levels:
         global LEVELS

@@ -339,10 +339,11 @@ __device__ __forceinline__ uint32_t add565(uint32_t c, int dr, int dg, int db) {
 }
 
 // Generic nearest-of-four indices (compute_indices, icbc.h:3179-3235).
+template <int UNROLL = 1>
 __device__ __forceinline__ uint32_t indices_generic(const float *row, V3 cw, const PalF &pal) {
     const V3 p0 = pal.c[0] * cw, p1 = pal.c[1] * cw, p2 = pal.c[2] * cw, p3 = pal.c[3] * cw;
     uint32_t out = 0;
-#pragma unroll 1
+#pragma unroll UNROLL
     for (int t = 0; t < 16; t++) {
         const V3 c = texel(row, t) * cw;
         const V3 t0 = c - p0, t1 = c - p1, t2 = c - p2, t3 = c - p3;
@@ -387,6 +388,56 @@ __device__ __forceinline__ float refine(const WarpCtx &w, const float *row, cons
     }
     return best;
 }
+
+// One block's refinement state, for refinement run one step at a time.
+struct RefineLane {
+    uint32_t c0, c1, idx, base_idx;
+    float best;
+    int i, last;
+};
+
+__device__ __forceinline__ void refine_begin(const WarpCtx &w, const float *row, const EncodeParams &p, float error,
+                                             uint32_t c0, uint32_t c1, uint32_t idx, RefineLane &s) {
+    s.c0 = c0;
+    s.c1 = c1;
+    s.idx = idx;
+    s.best = error;
+    s.i = 0;
+    s.last = 0;
+    s.base_idx = indices_generic<16>(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D));
+}
+
+// Iteration s.i of refine_endpoints (icbc.h:3614-3648), identical to one trip
+// of refine()'s loop.  Returns true when the loop would stop after it.
+__device__ __forceinline__ bool refine_step(const WarpCtx &w, const float *row, const EncodeParams &p, RefineLane &s) {
+    const int d = s.i & 15;
+    const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
+    uint32_t r0 = s.c0, r1 = s.c1;
+    if ((s.i >> 4) & 1) r0 = add565(r0, dr, dg, db);
+    else r1 = add565(r1, dr, dg, db);
+    if (!p.three_color_mode) {
+        if (r0 == r1) r1 = add565(r1, 0, 1, 0);
+        if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
+    }
+    const PalF pr = palette_f(r0, r1, p.decoder, w.T->lut255, w.D);
+    const float e = block_error<16>(row, p.cw, pr, s.base_idx);
+    if (e < s.best) {
+        s.best = e;
+        s.c0 = r0;
+        s.c1 = r1;
+        s.idx = s.base_idx;
+        s.last = s.i;
+        s.base_idx = indices_generic<16>(row, p.cw, pr);
+    }
+    s.i++;
+    return (s.i - 1 - s.last > 32) || s.i == 256;
+}
+
+// Per-block hand-over from the encode kernel to the refinement kernel.
+struct RefineSlot {
+    float error;       // compress_bc1's error before refinement
+    uint32_t pending;  // 1: refinement applies (two or more distinct colours)
+};
 
 // ---------------------------------------------------------- cluster fit --
 
@@ -614,10 +665,15 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 // the lanes that own a real block.  c0/c1/idx hold the caller's prior output
 // bytes on entry (levels 4..9 keep them when nothing is accepted) and the
 // encoded block on return; the return value is compress_bc1's error.
-template <int L>
-__device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
-                                             uint32_t &c1, uint32_t &idx) {
+//
+// With DEFER the refinement of level 9 is not run here: `refine_next` is set
+// for the blocks it applies to (the caller hands them to k_refine), and the
+// returned error is the one refinement starts from.
+template <int L, bool DEFER>
+__device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
+                                                uint32_t &c1, uint32_t &idx, bool &refine_next) {
     using O = Level<L>;
+    refine_next = false;
     const int lane = w.lane;
     const float *row = w.in + lane * kInStride;
     float *srow = w.sat + lane * kSatStride;
@@ -695,8 +751,18 @@ __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParam
         if (need4 && ferr < err) { c0 = f0; c1 = f1; idx = fi; err = ferr; }
     }
 
-    if (O::refine && live) err = refine(w, row, p, err, c0, c1, idx);
+    if (O::refine && live) {
+        if (DEFER) refine_next = true;
+        else err = refine(w, row, p, err, c0, c1, idx);
+    }
     return err;
+}
+
+template <int L>
+__device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
+                                             uint32_t &c1, uint32_t &idx) {
+    bool unused;
+    return encode_warp_ex<L, false>(w, p, active, c0, c1, idx, unused);
 }
 
 }  // namespace icbc_gpu

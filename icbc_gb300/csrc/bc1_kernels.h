@@ -66,6 +66,13 @@ cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder
 cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
                             cudaStream_t stream);
 
+// Level-9 refinement pass (bc1_refine.cu) and its stream-ordered scratch.
+cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream);
+cudaError_t scratch_free(void *ptr, cudaStream_t stream);
+cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
+                          const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
+                          unsigned long long *counter, cudaStream_t stream, int sms);
+
 // Host-side services of icbc_gpu_api.cu used by other translation units.
 const GlobalTables &host_tables();
 int ensure_tables_on_device(const GlobalTables **out);

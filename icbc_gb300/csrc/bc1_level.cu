@@ -15,9 +15,12 @@ namespace icbc_gpu {
 
 // ------------------------------------------------------------- kernels --
 
-template <int L>
+// With DEFER (level 9 only) refinement is left to k_refine: the kernel
+// records each block's starting error and whether refinement applies.
+template <int L, bool DEFER>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_blocks(const GlobalTables *G, BlocksSrc s, EncodeParams p,
-                                                                     uint2 *out, float *errors, int64_t n) {
+                                                                     uint2 *out, float *errors, int64_t n,
+                                                                     RefineSlot *st) {
     extern __shared__ __align__(16) unsigned char smem[];
     SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
     stage_tables(T, G);
@@ -39,16 +42,19 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_blocks(const Globa
             c1 = prev.x >> 16;
             idx = prev.y;
         }
-        const float e = encode_warp<L>(w, p, active, c0, c1, idx);
+        bool pending;
+        const float e = encode_warp_ex<L, DEFER>(w, p, active, c0, c1, idx, pending);
         if (active) {
             out[b] = make_uint2(c0 | (c1 << 16), idx);
             if (errors) errors[b] = e;
+            if (DEFER) st[b] = RefineSlot{e, pending ? 1u : 0u};
         }
     }
 }
 
-template <int L>
-__global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const GlobalTables *G, ImageDesc d, EncodeParams p) {
+template <int L, bool DEFER>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const GlobalTables *G, ImageDesc d, EncodeParams p,
+                                                                    RefineSlot *st) {
     extern __shared__ __align__(16) unsigned char smem[];
     SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
     stage_tables(T, G);
@@ -68,10 +74,12 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const Global
             c1 = prev.x >> 16;
             idx = prev.y;
         }
-        const float e = encode_warp<L>(w, p, active, c0, c1, idx);
+        bool pending;
+        const float e = encode_warp_ex<L, DEFER>(w, p, active, c0, c1, idx, pending);
         if (active) {
             d.out[b] = make_uint2(c0 | (c1 << 16), idx);
             if (d.errors) d.errors[b] = e;
+            if (DEFER) st[b] = RefineSlot{e, pending ? 1u : 0u};
         }
     }
 }
@@ -106,24 +114,56 @@ static int grid_for(K kernel, int64_t n, int sms) {
 #define ICBC_CAT2(a, b) a##b
 #define ICBC_CAT(a, b) ICBC_CAT2(a, b)
 
+// Level 9 encodes in two launches: the encoder without refinement, then
+// k_refine, handing over through a RefineSlot per block in stream-ordered
+// scratch.  Other levels are one launch.
+constexpr bool kDefer = Level<L>::refine;
+
+template <class Kernel, class Launch>
+static cudaError_t run(Kernel kernel, int64_t n, int sms, cudaStream_t stream, Launch launch,
+                       const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks, const EncodeParams &p,
+                       uint2 *out, float *errors) {
+    const size_t smem = smem_bytes(Level<L>::cluster);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = grid_for(kernel, n, sms);
+    if (!kDefer) {
+        launch(grid, smem, nullptr);
+        return cudaGetLastError();
+    }
+    const size_t slots = ((size_t)n * sizeof(RefineSlot) + 15) / 16 * 16;
+    void *scratch = nullptr;
+    e = scratch_alloc(&scratch, slots + 16, stream);
+    if (e != cudaSuccess) return e;
+    RefineSlot *st = reinterpret_cast<RefineSlot *>(scratch);
+    unsigned long long *counter = reinterpret_cast<unsigned long long *>(static_cast<char *>(scratch) + slots);
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+    if (e == cudaSuccess) {
+        launch(grid, smem, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = launch_refine(G, image, blocks, p, out, errors, st, n, counter, stream, sms);
+    const cudaError_t f = scratch_free(scratch, stream);
+    return e != cudaSuccess ? e : f;
+}
+
 cudaError_t ICBC_CAT(launch_blocks_l, ICBC_LEVEL)(const GlobalTables *G, const BlocksSrc &s, const EncodeParams &p,
                                                   void *out, float *errors, int64_t n, cudaStream_t stream, int sms) {
-    const size_t smem = smem_bytes(Level<L>::cluster);
-    cudaError_t e = cudaFuncSetAttribute(k_encode_blocks<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const int grid = grid_for(k_encode_blocks<L>, n, sms);
-    k_encode_blocks<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, s, p, reinterpret_cast<uint2 *>(out), errors, n);
-    return cudaGetLastError();
+    uint2 *o = reinterpret_cast<uint2 *>(out);
+    return run(k_encode_blocks<L, kDefer>, n, sms, stream,
+               [&](int grid, size_t smem, RefineSlot *st) {
+                   k_encode_blocks<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, s, p, o, errors, n, st);
+               },
+               G, nullptr, &s, p, o, errors);
 }
 
 cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
                                                  cudaStream_t stream, int sms) {
-    const size_t smem = smem_bytes(Level<L>::cluster);
-    cudaError_t e = cudaFuncSetAttribute(k_encode_image<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const int grid = grid_for(k_encode_image<L>, d.nblocks, sms);
-    k_encode_image<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p);
-    return cudaGetLastError();
+    return run(k_encode_image<L, kDefer>, d.nblocks, sms, stream,
+               [&](int grid, size_t smem, RefineSlot *st) {
+                   k_encode_image<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, st);
+               },
+               G, &d, nullptr, p, d.out, d.errors);
 }
 
 }  // namespace icbc_gpu

@@ -1,0 +1,156 @@
+// bc1_refine.cu -- endpoint refinement of level 9 as its own pass.
+//
+// refine_endpoints (icbc.h:3574-3651) runs 33 to 256 sequential steps per
+// block, different for every block.  Run inside the encoder, each lane
+// refines its own block and the warp waits for its slowest lane.  Here the
+// encoder leaves, per block, the error refinement starts from and whether it
+// applies (RefineSlot); this kernel then refines with a queue per lane: a
+// lane that finishes a block takes the next pending one (warp-aggregated
+// atomics on one counter), so lanes stay busy until the queue is empty.
+// Every step is the reference's step; only the scheduling differs.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "bc1_loaders.cuh"
+
+namespace icbc_gpu {
+
+// One float block (the compress_bc1 layout) into a lane's texel row.
+__device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_t b, float *row) {
+    const float4 *c = reinterpret_cast<const float4 *>(s.colors) + b * 16;
+#pragma unroll 4
+    for (int t = 0; t < 16; t++) {
+        const float4 v = __ldg(c + t);
+        row[4 * t + 0] = v.x;
+        row[4 * t + 1] = v.y;
+        row[4 * t + 2] = v.z;
+    }
+    if (s.weights) {
+        const float4 *w4 = reinterpret_cast<const float4 *>(s.weights) + b * 4;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float4 v = __ldg(w4 + j);
+            row[16 * j + 3] = v.x;
+            row[16 * j + 7] = v.y;
+            row[16 * j + 11] = v.z;
+            row[16 * j + 15] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < 16; t++) row[4 * t + 3] = 1.0f;
+    }
+}
+
+template <bool IMAGE>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables *G, ImageDesc d, BlocksSrc s,
+                                                              EncodeParams p, uint2 *out, float *errors,
+                                                              const RefineSlot *st, int64_t n,
+                                                              unsigned long long *counter) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    const WarpCtx w = warp_ctx<1>(smem, T, G, p.decoder);
+    const int lane = w.lane;
+    float *row = w.in + lane * kInStride;
+    RefineLane r;
+    int64_t blk = 0;
+    bool have = false, exhausted = false;
+    for (;;) {
+        // Lanes without a block take the next ones; blocks that need no
+        // refinement are skipped (their error and bytes are final already).
+        unsigned need = __ballot_sync(kFull, !have && !exhausted);
+        while (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(kFull, base, leader);
+            if (!have && !exhausted) {
+                const int64_t mine = (int64_t)base + __popc(need & ((1u << lane) - 1u));
+                if (mine >= n) {
+                    exhausted = true;
+                } else {
+                    const RefineSlot sl = st[mine];
+                    if (sl.pending) {
+                        if (IMAGE) load_image_block(d, mine, row, T.lut255);
+                        else load_float_block_lane(s, mine, row);
+                        const uint2 cur = out[mine];
+                        refine_begin(w, row, p, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
+                        blk = mine;
+                        have = true;
+                    }
+                }
+            }
+            need = __ballot_sync(kFull, !have && !exhausted);
+        }
+        if (!__any_sync(kFull, have)) break;
+        if (have && refine_step(w, row, p, r)) {
+            out[blk] = make_uint2(r.c0 | (r.c1 << 16), r.idx);
+            if (errors) errors[blk] = r.best;
+            have = false;
+        }
+    }
+}
+
+namespace {
+
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pool[64] = {};
+int g_refine_resident[2] = {0, 0};
+
+}  // namespace
+
+// Stream-ordered scratch from a library-owned pool of the current device
+// (freed memory stays cached in the pool for the next call).
+cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        if (!g_pool[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            e = cudaMemPoolCreate(&g_pool[dev], &props);
+            if (e != cudaSuccess) return e;
+            uint64_t keep = 1ull << 30;
+            cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool = g_pool[dev];
+    }
+    return cudaMallocFromPoolAsync(ptr, bytes, pool, stream);
+}
+
+cudaError_t scratch_free(void *ptr, cudaStream_t stream) { return cudaFreeAsync(ptr, stream); }
+
+cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
+                          const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
+                          unsigned long long *counter, cudaStream_t stream, int sms) {
+    const size_t smem = smem_bytes(false);
+    const bool img = image != nullptr;
+    cudaError_t e = img ? cudaFuncSetAttribute(k_refine<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(k_refine<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int &resident = g_refine_resident[img ? 1 : 0];
+    if (!resident) {
+        int per_sm = 0;
+        e = img ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine<true>, kWarpsPerCta * 32, smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine<false>, kWarpsPerCta * 32, smem);
+        if (e != cudaSuccess) return e;
+        resident = per_sm > 0 ? per_sm : 1;
+    }
+    const int64_t want = (n + kWarpsPerCta * 32 - 1) / (kWarpsPerCta * 32);
+    const int64_t cap = (int64_t)sms * resident;
+    const int grid = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+    ImageDesc dd = img ? *image : ImageDesc{};
+    BlocksSrc ss = blocks ? *blocks : BlocksSrc{nullptr, nullptr};
+    if (img) k_refine<true><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, dd, ss, p, out, errors, st, n, counter);
+    else k_refine<false><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, dd, ss, p, out, errors, st, n, counter);
+    return cudaGetLastError();
+}
+
+}  // namespace icbc_gpu

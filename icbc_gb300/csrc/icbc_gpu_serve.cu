@@ -202,8 +202,11 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
                             slot.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(slot.d_counter, 0, sizeof(int), slot.stream);
     if (e == cudaSuccess)
+        // A persistent grid no larger than the batch's work (four tasks per
+        // CTA at least), so small batches share the GPU instead of each
+        // filling it.
         e = launch_encode_batch(S->G, slot.d_images, nullptr, slot.d_start, n, (int)total, slot.d_counter,
-                                slot.stream, S->grid);
+                                slot.stream, (int)std::min<uint32_t>((uint32_t)S->grid, (total + 3) / 4));
     for (size_t i = 0; i < reqs.size() && e == cudaSuccess; i++) {
         Request *q = reqs[i];
         const ImageDesc &d = slot.h_images[i];

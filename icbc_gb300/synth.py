@@ -224,3 +224,41 @@ def mixed_blocks(n: int, seed: int = 3) -> tuple[np.ndarray, np.ndarray]:
     colors = lut[tex].astype(np.float32)
     colors[:, :, 3] = 1.0
     return np.ascontiguousarray(colors), np.ascontiguousarray(lut[tex[:, :, 3]])
+
+
+def hard_mixture_torch(w: int, h: int, seed: int, device="cuda"):
+    """The hard block mixture of ``hard_mixture_image`` generated on the GPU
+    with torch's seeded generator (for the 64 x 8192^2 workload, where host
+    generation would dominate).  Same mixture and weights; different random
+    stream, so compare results only against the same tensor's contents.
+    w and h must be multiples of 4."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    bw, bh = w // 4, h // 4
+
+    def rnd(*shape):
+        return torch.rand(shape, generator=g, device=device)
+
+    def rint(lo, hi, *shape):
+        return torch.randint(lo, hi, shape, generator=g, device=device, dtype=torch.int16)
+
+    kind = rnd(bh, 1, bw, 1, 1)
+    ca, cb = rint(0, 256, bh, 1, bw, 1, 3), rint(0, 256, bh, 1, bw, 1, 3)
+    out = rint(0, 256, bh, 4, bw, 4, 3)                                       # i.i.d. noise
+    dither = torch.where(rnd(bh, 4, bw, 4, 1) < 0.5, ca, cb)
+    out = torch.where((kind >= 0.30) & (kind < 0.50), dither, out)
+    del dither
+    out = torch.where((kind >= 0.50) & (kind < 0.65), ca.expand(bh, 4, bw, 4, 3), out)
+    dark = torch.where(rnd(bh, 4, bw, 4, 1) < 0.5, rint(0, 9, bh, 4, bw, 4, 3), rint(0, 32, bh, 4, bw, 4, 3))
+    out = torch.where((kind >= 0.65) & (kind < 0.80), dark, out)
+    del dark
+    gr = torch.arange(4, device=device, dtype=torch.float32) / 3.0
+    t = 0.5 * gr.view(1, 1, 1, 4, 1) + 0.5 * gr.view(1, 4, 1, 1, 1)
+    grad = ca.float() + (cb.float() - ca.float()) * t + 24.0 * (rnd(bh, 4, bw, 4, 3) - 0.5)
+    grad = torch.floor(grad + 0.5).clamp(0, 255).to(torch.int16)
+    out = torch.where(kind >= 0.80, grad, out)
+    del grad
+    alpha = torch.where(rnd(bh, 4, bw, 4, 1) < 0.25, 0, 255).to(torch.int16)
+    img = torch.cat([out, alpha], dim=-1).to(torch.uint8)
+    return img.reshape(bh * 4, bw * 4, 4).contiguous()
