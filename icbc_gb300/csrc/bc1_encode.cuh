@@ -404,7 +404,7 @@ __device__ __forceinline__ void refine_begin(const WarpCtx &w, const float *row,
     s.best = error;
     s.i = 0;
     s.last = 0;
-    s.base_idx = indices_generic<16>(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D));
+    s.base_idx = indices_generic<4>(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D));
 }
 
 // Iteration s.i of refine_endpoints (icbc.h:3614-3648), identical to one trip
@@ -420,14 +420,14 @@ __device__ __forceinline__ bool refine_step(const WarpCtx &w, const float *row, 
         if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
     }
     const PalF pr = palette_f(r0, r1, p.decoder, w.T->lut255, w.D);
-    const float e = block_error<16>(row, p.cw, pr, s.base_idx);
+    const float e = block_error<4>(row, p.cw, pr, s.base_idx);
     if (e < s.best) {
         s.best = e;
         s.c0 = r0;
         s.c1 = r1;
         s.idx = s.base_idx;
         s.last = s.i;
-        s.base_idx = indices_generic<16>(row, p.cw, pr);
+        s.base_idx = indices_generic<4>(row, p.cw, pr);
     }
     s.i++;
     return (s.i - 1 - s.last > 32) || s.i == 256;
