@@ -158,6 +158,21 @@ def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=None):
     return times, stats, outs
 
 
+def max_over_ranks(value: float, device) -> float:
+    """The largest of every rank's value (the job's time is its slowest rank)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gpix(world: int, pixels_per_rank: float, step_ms_max: float) -> float:
+    """Whole-job Gpixel/s: every rank encodes its own replica of the step's
+    pixels; the step takes as long as the slowest rank."""
+    return world * pixels_per_rank / (step_ms_max * 1e-3) / 1e9
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -229,6 +244,14 @@ def run_ours(args):
     def encode(lv):
         ig.compress_image(d_img, lv, ig.Decoder_D3D10, CW, weight_mode=ig.WEIGHTS_ALPHA, out=outs[lv], stream=stream)
 
+    # Launch shapes per level picked by the autotuner on this workload (outside
+    # the timed region).
+    tuning = None
+    if not args.no_autotune:
+        table = ig.autotune(d_img, LEVELS, color_weights=CW, weight_mode=ig.WEIGHTS_ALPHA)
+        tuning = {str(lv): "%d groups/warp, %s" % (t["groups_per_warp"], "persistent" if t["persistent"] else
+                                                    "hw-balanced") for lv, t in table.items()}
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             for lv in LEVELS:
@@ -260,11 +283,8 @@ def run_ours(args):
     lvl_ms = {lv: statistics.mean(ev[k][i][0].elapsed_time(ev[k][i][1]) for k in range(args.steps))
               for i, lv in enumerate(LEVELS)}
     step_ms = sum(lvl_ms.values())
-    if ws > 1:
-        t = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = ws * len(LEVELS) * px / (step_ms * 1e-3) / 1e9
+    step_ms = max_over_ranks(step_ms, dev) if ws > 1 else step_ms
+    value = whole_job_gpix(ws, len(LEVELS) * px, step_ms)
 
     # End to end through the host-buffer C-ABI call: pinned image in, blocks out.
     e2e_value = h2d = d2h = None
@@ -327,6 +347,7 @@ def run_ours(args):
                          "sample": "every %dth block row (%d px) at all 10 levels" % (args.cpu_stride, sample_px)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step"},
+        "autotune": tuning,
         "batch": batch,
         "serving": serving,
         "hard": hard,
@@ -567,6 +588,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-hard", action="store_true", help="skip the hard-distribution leg")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--hard-images", type=int, default=64)
     ap.add_argument("--hard-side", type=int, default=8192)
     ap.add_argument("--hard-steps", type=int, default=2)

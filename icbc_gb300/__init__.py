@@ -48,6 +48,11 @@ class ImageDesc(ctypes.Structure):
                 ("color_weights", ctypes.c_float * 3), ("out", ctypes.c_void_p), ("errors", ctypes.c_void_p)]
 
 
+class LaunchConfig(ctypes.Structure):
+    """struct icbc_gpu_launch_config."""
+    _fields_ = [("groups_per_warp", ctypes.c_int32), ("persistent", ctypes.c_int32)]
+
+
 class ServerConfig(ctypes.Structure):
     """struct icbc_gpu_server_config."""
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_inflight", ctypes.c_int32),
@@ -120,6 +125,11 @@ def load(build_if_missing: bool = True):
             "icbc_gpu_server_cancel": (i32, [vp, ctypes.c_uint64]),
             "icbc_gpu_server_get_stats": (i32, [vp, ctypes.POINTER(ServerStats)]),
             "icbc_gpu_server_destroy": (i32, [vp]),
+            "icbc_gpu_write_dds": (i32, [ctypes.c_char_p, i32, i32, vp]),
+            "icbc_gpu_set_launch_config": (i32, [i32, ctypes.POINTER(LaunchConfig)]),
+            "icbc_gpu_get_launch_config": (i32, [i32, ctypes.POINTER(LaunchConfig)]),
+            "icbc_gpu_write_ktx": (i32, [ctypes.c_char_p, i32, i32, vp]),
+            "icbc_gpu_compare_dds": (i32, [ctypes.c_char_p, i32, i32, vp]),
             "icbc_gpu_compress_bc1_images_noalloc": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
         }
         for name, (res, args) in sig.items():
@@ -384,6 +394,31 @@ def compress_image_host(rgba: np.ndarray, level: int, decoder: int = DECODER_DEF
     return out
 
 
+def _blocks_ptr(blocks):
+    return blocks.data_ptr() if hasattr(blocks, "data_ptr") else np.ascontiguousarray(blocks, np.uint8).ctypes.data
+
+
+def write_dds(path: str, width: int, height: int, blocks) -> None:
+    """DDS file (DXT1, one mip) of host (numpy) or device (torch) blocks."""
+    b = blocks if hasattr(blocks, "data_ptr") else np.ascontiguousarray(blocks, np.uint8)
+    _check(load().icbc_gpu_write_dds(os.fsencode(path), int(width), int(height), _blocks_ptr(b)), "write_dds")
+
+
+def write_ktx(path: str, width: int, height: int, blocks) -> None:
+    """KTX 1.1 file (GL_COMPRESSED_RGB_S3TC_DXT1_EXT) of host or device blocks."""
+    b = blocks if hasattr(blocks, "data_ptr") else np.ascontiguousarray(blocks, np.uint8)
+    _check(load().icbc_gpu_write_ktx(os.fsencode(path), int(width), int(height), _blocks_ptr(b)), "write_ktx")
+
+
+def compare_dds(path: str, width: int, height: int, blocks) -> bool:
+    """Golden-file check: True when the DDS file holds exactly these blocks."""
+    b = blocks if hasattr(blocks, "data_ptr") else np.ascontiguousarray(blocks, np.uint8)
+    r = load().icbc_gpu_compare_dds(os.fsencode(path), int(width), int(height), _blocks_ptr(b))
+    if r < 0:
+        raise IcbcGpuError(-r, "compare_dds")
+    return r == 1
+
+
 class Server:
     """The serving form (icbc_gpu_server_*): submit host RGBA8 images as they
     arrive; they are admitted under the HBM budget and batched onto the GPU.
@@ -446,3 +481,66 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- autotuner
+
+TUNE_CANDIDATES = [(g, p) for p in (0, 1) for g in (1, 2, 4, 8)]
+
+
+def get_launch_config(level: int) -> tuple[int, int]:
+    c = LaunchConfig()
+    _check(load().icbc_gpu_get_launch_config(int(level), ctypes.byref(c)), "get_launch_config")
+    return c.groups_per_warp, c.persistent
+
+
+def set_launch_config(level: int, groups_per_warp: int, persistent: int) -> None:
+    c = LaunchConfig(int(groups_per_warp), int(persistent))
+    _check(load().icbc_gpu_set_launch_config(int(level), ctypes.byref(c)), "set_launch_config")
+
+
+def autotune(image, levels=range(10), candidates=TUNE_CANDIDATES, repeats: int = 3, decoder: int = Decoder_D3D10,
+             color_weights=(1.0, 1.0, 1.0), weight_mode: int = WEIGHTS_UNIFORM, apply: bool = True,
+             path: str | None = None) -> dict:
+    """Times every launch shape of the plain image kernel on `image` (a CUDA
+    uint8 tensor (h, w, 4)) for each level with CUDA events, keeps the fastest
+    (applied to the library when `apply`), and returns
+    {level: {"groups_per_warp", "persistent", "ms", "candidates": {...}}}.
+    With `path` the table is also written as JSON (load_tuning reads it)."""
+    import json
+    torch = _torch()
+    nb = blocks_of(int(image.shape[1]), int(image.shape[0]))
+    out = torch.zeros((nb, 8), dtype=torch.uint8, device=image.device)
+    stream = torch.cuda.Stream(device=image.device)
+    table = {}
+    for lv in levels:
+        before = get_launch_config(lv)
+        times = {}
+        for g, p in candidates:
+            set_launch_config(lv, g, p)
+            with torch.cuda.stream(stream):
+                compress_image(image, lv, decoder, color_weights, weight_mode, out=out, stream=stream)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(repeats):
+                    compress_image(image, lv, decoder, color_weights, weight_mode, out=out, stream=stream)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            times["%d/%d" % (g, p)] = e0.elapsed_time(e1) / repeats
+        best = min(times, key=times.get)
+        g, p = (int(x) for x in best.split("/"))
+        set_launch_config(lv, *((g, p) if apply else before))
+        table[int(lv)] = {"groups_per_warp": g, "persistent": p, "ms": times[best], "candidates": times}
+    if path:
+        with open(path, "w") as f:
+            json.dump({str(k): v for k, v in table.items()}, f, indent=1)
+    return table
+
+
+def load_tuning(path: str) -> None:
+    """Applies a table written by autotune(path=...)."""
+    import json
+    with open(path) as f:
+        table = json.load(f)
+    for lv, cfg in table.items():
+        set_launch_config(int(lv), cfg["groups_per_warp"], cfg["persistent"])

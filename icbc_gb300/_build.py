@@ -39,7 +39,7 @@ def _units():
              for lv in range(10)]
     units += [(os.path.join(CSRC, n), [], n.replace(".cu", ".o"))
               for n in ("bc1_batch.cu", "bc1_decode.cu", "icbc_gpu_api.cu", "icbc_gpu_serve.cu",
-                        "icbc_compat.cu", "bc1_noalloc.cu", "bc1_refine.cu")]
+                        "icbc_compat.cu", "bc1_noalloc.cu", "bc1_refine.cu", "icbc_containers.cu")]
     return [u for u in units if os.path.exists(u[0])]
 
 

@@ -73,6 +73,13 @@ cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const B
                           const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
                           unsigned long long *counter, cudaStream_t stream, int sms);
 
+// Launch shape of the plain kernels of a level (autotuned or default).
+struct LaunchShape {
+    int groups_per_warp;
+    bool persistent;
+};
+LaunchShape launch_shape(int level);
+
 // Host-side services of icbc_gpu_api.cu used by other translation units.
 const GlobalTables &host_tables();
 int ensure_tables_on_device(const GlobalTables **out);

@@ -86,29 +86,32 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const Global
 
 constexpr int L = ICBC_LEVEL;
 
-// CTAs for n blocks.  Levels 0-1 cost the same for every block: the grid is
-// exactly the resident CTAs (from the occupancy API), each warp striding
-// over groups of 32 blocks, so there is no partial last wave and the per-CTA
-// table staging is paid once per resident CTA.  Levels 2-9 cost depends on
-// the data: two groups per warp and many CTAs, balanced by the hardware.
+// CTAs for n blocks, from the level's launch shape: every warp takes
+// groups_per_warp groups of 32 blocks; a persistent grid is exactly the
+// resident CTAs (from the occupancy API), each warp striding over the image,
+// otherwise there are enough CTAs for the work and the hardware balances
+// them (better when block costs vary, as they do from level 2 on).
 template <class K>
 static int grid_for(K kernel, int64_t n, int sms) {
+    const LaunchShape shape = launch_shape(L);
     const int64_t groups = (n + 31) / 32;
-    const int64_t per_cta = (int64_t)kWarpsPerCta * (Level<L>::cluster ? 2 : 1);
+    const int64_t per_cta = (int64_t)kWarpsPerCta * shape.groups_per_warp;
     int64_t ctas = (groups + per_cta - 1) / per_cta;
-    if (!Level<L>::cluster) {
+    if (shape.persistent) {
         static int resident = 0;
         if (!resident) {
             int per_sm = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerCta * 32,
-                                                              smem_bytes(false)) != cudaSuccess || per_sm < 1)
+                                                              smem_bytes(Level<L>::cluster)) != cudaSuccess ||
+                per_sm < 1)
                 per_sm = 1;
             resident = per_sm;
         }
         const int64_t cap = (int64_t)sms * resident;
-        ctas = ctas < cap ? ctas : cap;
+        const int64_t all = (groups + kWarpsPerCta - 1) / kWarpsPerCta;
+        ctas = all < cap ? all : cap;
     }
-    return (int)(ctas < 0x7fffffff ? ctas : 0x7fffffff);
+    return (int)(ctas < 1 ? 1 : ctas < 0x7fffffff ? ctas : 0x7fffffff);
 }
 
 #define ICBC_CAT2(a, b) a##b

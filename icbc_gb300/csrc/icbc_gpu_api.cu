@@ -256,6 +256,15 @@ static const int kLevelCost[10] = {1, 2, 6, 8, 12, 14, 16, 17, 20, 26};
 
 namespace icbc_gpu {
 int level_cost(int level) { return kLevelCost[level < 0 ? 0 : level > 9 ? 9 : level]; }
+
+// Per-level launch shapes of the plain kernels (see icbc_gpu_launch_config).
+static icbc_gpu_launch_config g_launch[10] = {{1, 1}, {1, 1}, {2, 0}, {2, 0}, {2, 0},
+                                             {2, 0}, {2, 0}, {2, 0}, {2, 0}, {2, 0}};
+
+LaunchShape launch_shape(int level) {
+    const icbc_gpu_launch_config c = g_launch[level < 0 ? 0 : level > 9 ? 9 : level];
+    return LaunchShape{c.groups_per_warp, c.persistent != 0};
+}
 }  // namespace icbc_gpu
 
 struct icbc_gpu_batch {
@@ -307,6 +316,20 @@ const char *icbc_gpu_status_string(int status) {
 const char *icbc_gpu_last_error(void) { return t_last_error.c_str(); }
 
 int icbc_gpu_sm_count(void) { return sm_count(); }
+
+int icbc_gpu_set_launch_config(int level, const icbc_gpu_launch_config *config) {
+    if (level < 0 || level > 9 || !config || config->groups_per_warp < 1 || config->groups_per_warp > 64)
+        return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    g_launch[level] = *config;
+    g_launch[level].persistent = config->persistent ? 1 : 0;
+    return ICBC_GPU_OK;
+}
+
+int icbc_gpu_get_launch_config(int level, icbc_gpu_launch_config *config) {
+    if (level < 0 || level > 9 || !config) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    *config = g_launch[level];
+    return ICBC_GPU_OK;
+}
 
 int icbc_gpu_debug_tables(int decoder, uint8_t match5[512], uint8_t match6[512], float weights[5], uint32_t four[968],
                           int32_t four_total[16], uint32_t three[152], int32_t three_total[16]) {

@@ -241,6 +241,34 @@ int icbc_gpu_server_get_stats(icbc_gpu_server *server, icbc_gpu_server_stats *st
  * Must not run concurrently with other calls on the same server. */
 int icbc_gpu_server_destroy(icbc_gpu_server *server);
 
+/* ------------------------------------------------------------------------
+ * Containers for encoded images (icbc_test.cpp:155-279).  `blocks` are
+ * ceil(w/4) * ceil(h/4) BC1 blocks in row-major block order, in host or
+ * device memory (device blocks are copied out first).  Headers hold the
+ * image's own width and height; the data size is 8 bytes per block.
+ * ---------------------------------------------------------------------- */
+/* DDS with a DXT1 FourCC and one mip level (icbc_test.cpp:155-211). */
+int icbc_gpu_write_dds(const char *path, int32_t width, int32_t height, const void *blocks);
+/* KTX 1.1, GL_COMPRESSED_RGB_S3TC_DXT1_EXT (icbc_test.cpp:233-279). */
+int icbc_gpu_write_ktx(const char *path, int32_t width, int32_t height, const void *blocks);
+/* Golden-file check (icbc_test.cpp:213-231): 1 when the DDS file's block
+ * data equals `blocks`, 0 when it differs, a negative status on error
+ * (-ICBC_GPU_ERR_NOT_FOUND: file missing or short). */
+int icbc_gpu_compare_dds(const char *path, int32_t width, int32_t height, const void *blocks);
+
+/* Launch shape of the plain kernels of one quality level, chosen by an
+ * autotuner (icbc_gb300.autotune) or set by hand.  groups_per_warp: groups
+ * of 32 blocks each warp takes (1..64); persistent: 1 = exactly the
+ * resident CTAs, striding over the image, 0 = enough CTAs for the work,
+ * balanced by the hardware.  Defaults: 1 / persistent at levels 0-1,
+ * 2 / not persistent at levels 2-9.  Not for use while launches run. */
+typedef struct icbc_gpu_launch_config {
+    int32_t groups_per_warp;
+    int32_t persistent;
+} icbc_gpu_launch_config;
+int icbc_gpu_set_launch_config(int level, const icbc_gpu_launch_config *config);
+int icbc_gpu_get_launch_config(int level, icbc_gpu_launch_config *config);
+
 /* Number of SMs of the current device (for sizing host-side work). */
 int icbc_gpu_sm_count(void);
 

@@ -210,3 +210,26 @@ def test_full_size_sampled_parity(gpu_lib, level):
     assert same_bits(e[idx], oe)
     mse = e.astype(np.float64).sum() / (16 * blocks.shape[0])
     assert 20 * np.log10(255 / np.sqrt(mse)) > 30
+
+
+def test_launch_shapes_do_not_change_results(gpu_lib):
+    """Every launch shape the autotuner may pick gives the same bytes, and
+    autotune() applies and reports a valid shape per level."""
+    import torch
+    ig = gpu_lib
+    img = _to_dev(synth.quality_sweep_image(320, 200, seed=4))
+    saved = {lv: ig.get_launch_config(lv) for lv in range(10)}
+    try:
+        for lv in (0, 5, 9):
+            ref = ig.compress_image(img, lv, 0, (1, 1, 1), weight_mode=ig.WEIGHTS_ALPHA).cpu().numpy()
+            for g, p in ig.TUNE_CANDIDATES:
+                ig.set_launch_config(lv, g, p)
+                out = ig.compress_image(img, lv, 0, (1, 1, 1), weight_mode=ig.WEIGHTS_ALPHA).cpu().numpy()
+                assert np.array_equal(out, ref), (lv, g, p)
+        table = ig.autotune(img, levels=(1, 8), repeats=1)
+        for lv in (1, 8):
+            assert (table[lv]["groups_per_warp"], table[lv]["persistent"]) == ig.get_launch_config(lv)
+            assert len(table[lv]["candidates"]) == len(ig.TUNE_CANDIDATES)
+    finally:
+        for lv, (g, p) in saved.items():
+            ig.set_launch_config(lv, g, p)
