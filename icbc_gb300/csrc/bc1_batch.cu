@@ -11,10 +11,14 @@ namespace icbc_gpu {
 // ordered most expensive level first by the planner.  A task is either an
 // entry of an explicit list (`tasks`), or -- when `tasks` is NULL -- found from
 // per-image offsets: task t belongs to the last image whose first task
-// (`task_start[i]`, n_images + 1 entries) is <= t.
+// (`task_start[i]`, n_images + 1 entries) is <= t.  With `refine_base`, the
+// level-9 images leave refinement to k_refine's batch mode (bc1_refine.cu),
+// which runs after this kernel in the same stream: the same split as the
+// plain level-9 launches, so lanes do not wait for each other's refinement.
 __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const GlobalTables *G, const ImageDesc *images,
                                                                      const BatchTask *tasks, const uint32_t *task_start,
-                                                                     int n_images, int ntasks, int *counter) {
+                                                                     int n_images, int ntasks, int *counter,
+                                                                     const int64_t *refine_base, RefineSlot *slots) {
     extern __shared__ __align__(16) unsigned char smem[];
     SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
     stage_tables(T, G);
@@ -57,6 +61,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
             c1 = prev.x >> 16;
             idx = prev.y;
         }
+        // Level 9 with a refinement slot range: encode now, refine in
+        // k_refine's batch mode (warp-uniform: one image per task).
+        const int64_t base = (level == 9 && refine_base) ? refine_base[task.image] : -1;
+        bool pending = false;
         float e = 0.0f;
         switch (level) {
             case 0: e = encode_warp<0>(w, p, active, c0, c1, idx); break;
@@ -68,22 +76,27 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
             case 6: e = encode_warp<6>(w, p, active, c0, c1, idx); break;
             case 7: e = encode_warp<7>(w, p, active, c0, c1, idx); break;
             case 8: e = encode_warp<8>(w, p, active, c0, c1, idx); break;
-            default: e = encode_warp<9>(w, p, active, c0, c1, idx); break;
+            default:
+                if (base >= 0) e = encode_warp_ex<9, true>(w, p, active, c0, c1, idx, pending);
+                else e = encode_warp<9>(w, p, active, c0, c1, idx);
+                break;
         }
         if (active) {
             d.out[b] = make_uint2(c0 | (c1 << 16), idx);
             if (d.errors) d.errors[b] = e;
+            if (base >= 0) slots[base + b] = RefineSlot{e, pending ? 1u : 0u};
         }
     }
 }
 
 cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
                                 const uint32_t *task_start, int n_images, int ntasks, int *counter,
-                                cudaStream_t stream, int grid) {
+                                cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots) {
     const size_t smem = smem_bytes(true);
     cudaError_t e = cudaFuncSetAttribute(k_encode_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_encode_batch<<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, task_start, n_images, ntasks, counter);
+    k_encode_batch<<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, task_start, n_images, ntasks, counter,
+                                                               refine_base, slots);
     return cudaGetLastError();
 }
 

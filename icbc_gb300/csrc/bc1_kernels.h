@@ -58,9 +58,13 @@ ICBC_DECLARE_LEVEL(8)
 ICBC_DECLARE_LEVEL(9)
 #undef ICBC_DECLARE_LEVEL
 
+// With refine_base (one entry per image; -1: refine inline) a level-9 image's
+// refinement is deferred: block b's RefineSlot goes to slots[refine_base[i] + b]
+// and launch_refine_batch finishes it.  NULL refine_base: all inline.
 cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
                                 const uint32_t *task_start, int n_images, int ntasks, int *counter,
-                                cudaStream_t stream, int grid);
+                                cudaStream_t stream, int grid, const int64_t *refine_base = nullptr,
+                                RefineSlot *slots = nullptr);
 int batch_ctas_per_sm();
 cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder, cudaStream_t stream);
 cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
@@ -72,6 +76,18 @@ cudaError_t scratch_free(void *ptr, cudaStream_t stream);
 cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
                           const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
                           unsigned long long *counter, cudaStream_t stream, int sms);
+
+// The deferred level-9 blocks of a batch: refinement index r belongs to image
+// map_image[k] for the k with map_start[k] <= r < map_start[k + 1] (n + 1
+// entries), block r - map_start[k]; slots[r] is its hand-over.
+struct RefineMap {
+    const int64_t *map_start;
+    const uint32_t *map_image;
+    int n;
+};
+cudaError_t launch_refine_batch(const GlobalTables *G, const ImageDesc *images, RefineMap map,
+                                const RefineSlot *slots, int64_t total, unsigned long long *counter,
+                                cudaStream_t stream, int sms);
 
 // Launch shape of the plain kernels of a level (autotuned or default).
 struct LaunchShape {

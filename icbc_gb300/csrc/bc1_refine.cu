@@ -42,19 +42,25 @@ __device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_
     }
 }
 
-template <bool IMAGE>
+// MODE 0: float blocks (s), 1: one image (d), 2: the deferred level-9 blocks
+// of a batch (images + map), each lane with its own image's decoder and
+// parameters.
+template <int MODE>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables *G, ImageDesc d, BlocksSrc s,
                                                               EncodeParams p, uint2 *out, float *errors,
                                                               const RefineSlot *st, int64_t n,
-                                                              unsigned long long *counter) {
+                                                              unsigned long long *counter, const ImageDesc *images,
+                                                              RefineMap map) {
     extern __shared__ __align__(16) unsigned char smem[];
     SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
     stage_tables(T, G);
-    const WarpCtx w = warp_ctx<1>(smem, T, G, p.decoder);
+    WarpCtx w = warp_ctx<1>(smem, T, G, p.decoder);
     const int lane = w.lane;
     float *row = w.in + lane * kInStride;
+    EncodeParams lp = p;
     RefineLane r;
-    int64_t blk = 0;
+    uint2 *o = nullptr;
+    float *er = nullptr;
     bool have = false, exhausted = false;
     for (;;) {
         // Lanes without a block take the next ones; blocks that need no
@@ -72,11 +78,31 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
                 } else {
                     const RefineSlot sl = st[mine];
                     if (sl.pending) {
-                        if (IMAGE) load_image_block(d, mine, row, T.lut255);
-                        else load_float_block_lane(s, mine, row);
-                        const uint2 cur = out[mine];
-                        refine_begin(w, row, p, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
-                        blk = mine;
+                        if (MODE == 2) {
+                            int lo = 0, hi = map.n;
+                            while (hi - lo > 1) {
+                                const int mid = (lo + hi) >> 1;
+                                if (map.map_start[mid] <= mine) lo = mid;
+                                else hi = mid;
+                            }
+                            const ImageDesc &di = images[map.map_image[lo]];
+                            const int64_t b = mine - map.map_start[lo];
+                            lp.decoder = di.decoder;
+                            lp.three_color_mode = di.three_color_mode;
+                            lp.three_color_black = di.three_color_black;
+                            lp.cw = v3(di.cw[0], di.cw[1], di.cw[2]);
+                            w.D = &G->dec[di.decoder];
+                            load_image_block(di, b, row, T.lut255);
+                            o = di.out + b;
+                            er = di.errors ? di.errors + b : nullptr;
+                        } else {
+                            if (MODE == 1) load_image_block(d, mine, row, T.lut255);
+                            else load_float_block_lane(s, mine, row);
+                            o = out + mine;
+                            er = errors ? errors + mine : nullptr;
+                        }
+                        const uint2 cur = *o;
+                        refine_begin(w, row, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
                         have = true;
                     }
                 }
@@ -84,9 +110,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
             need = __ballot_sync(kFull, !have && !exhausted);
         }
         if (!__any_sync(kFull, have)) break;
-        if (have && refine_step(w, row, p, r)) {
-            out[blk] = make_uint2(r.c0 | (r.c1 << 16), r.idx);
-            if (errors) errors[blk] = r.best;
+        if (have && refine_step(w, row, lp, r)) {
+            *o = make_uint2(r.c0 | (r.c1 << 16), r.idx);
+            if (er) *er = r.best;
             have = false;
         }
     }
@@ -96,7 +122,6 @@ namespace {
 
 std::mutex g_pool_mutex;
 cudaMemPool_t g_pool[64] = {};
-int g_refine_resident[2] = {0, 0};
 
 }  // namespace
 
@@ -127,29 +152,50 @@ cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream) {
 
 cudaError_t scratch_free(void *ptr, cudaStream_t stream) { return cudaFreeAsync(ptr, stream); }
 
-cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
-                          const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
-                          unsigned long long *counter, cudaStream_t stream, int sms) {
-    const size_t smem = smem_bytes(false);
-    const bool img = image != nullptr;
-    cudaError_t e = img ? cudaFuncSetAttribute(k_refine<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                        : cudaFuncSetAttribute(k_refine<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int MODE>
+static cudaError_t refine_grid(int64_t n, int sms, size_t smem, int *grid) {
+    static int resident = 0;
+    cudaError_t e = cudaFuncSetAttribute(k_refine<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int &resident = g_refine_resident[img ? 1 : 0];
     if (!resident) {
         int per_sm = 0;
-        e = img ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine<true>, kWarpsPerCta * 32, smem)
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine<false>, kWarpsPerCta * 32, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_refine<MODE>, kWarpsPerCta * 32, smem);
         if (e != cudaSuccess) return e;
         resident = per_sm > 0 ? per_sm : 1;
     }
     const int64_t want = (n + kWarpsPerCta * 32 - 1) / (kWarpsPerCta * 32);
     const int64_t cap = (int64_t)sms * resident;
-    const int grid = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-    ImageDesc dd = img ? *image : ImageDesc{};
-    BlocksSrc ss = blocks ? *blocks : BlocksSrc{nullptr, nullptr};
-    if (img) k_refine<true><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, dd, ss, p, out, errors, st, n, counter);
-    else k_refine<false><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, dd, ss, p, out, errors, st, n, counter);
+    *grid = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+    return cudaSuccess;
+}
+
+cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
+                          const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
+                          unsigned long long *counter, cudaStream_t stream, int sms) {
+    const size_t smem = smem_bytes(false);
+    const ImageDesc dd = image ? *image : ImageDesc{};
+    const BlocksSrc ss = blocks ? *blocks : BlocksSrc{nullptr, nullptr};
+    const RefineMap none{nullptr, nullptr, 0};
+    int grid = 0;
+    cudaError_t e = image ? refine_grid<1>(n, sms, smem, &grid) : refine_grid<0>(n, sms, smem, &grid);
+    if (e != cudaSuccess) return e;
+    if (image)
+        k_refine<1><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, dd, ss, p, out, errors, st, n, counter, nullptr, none);
+    else
+        k_refine<0><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, dd, ss, p, out, errors, st, n, counter, nullptr, none);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_batch(const GlobalTables *G, const ImageDesc *images, RefineMap map,
+                                const RefineSlot *slots, int64_t total, unsigned long long *counter,
+                                cudaStream_t stream, int sms) {
+    const size_t smem = smem_bytes(false);
+    int grid = 0;
+    cudaError_t e = refine_grid<2>(total, sms, smem, &grid);
+    if (e != cudaSuccess) return e;
+    EncodeParams p{};
+    k_refine<2><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, ImageDesc{}, BlocksSrc{nullptr, nullptr}, p, nullptr,
+                                                           nullptr, slots, total, counter, images, map);
     return cudaGetLastError();
 }
 

@@ -273,6 +273,15 @@ struct icbc_gpu_batch {
     int *d_counter = nullptr;
     int ntasks = 0;
     int grid = 0;
+    // Level-9 images refine in a second launch (k_refine's batch mode):
+    // per-image slot base (-1: none), the refinement map, the slots, a counter.
+    int64_t *d_refine_base = nullptr;
+    int64_t *d_map_start = nullptr;
+    uint32_t *d_map_image = nullptr;
+    RefineSlot *d_slots = nullptr;
+    unsigned long long *d_refine_counter = nullptr;
+    int64_t refine_total = 0;
+    int map_n = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -413,9 +422,23 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     for (int i : order)
         for (int64_t b = 0; b < descs[i].nblocks; b += 32) tasks.push_back(BatchTask{(uint32_t)i, (uint32_t)b});
     if (tasks.size() > 0x7fffffff) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    // Refinement slots of the level-9 images, in task order.
+    std::vector<int64_t> refine_base((size_t)n_images, -1), map_start;
+    std::vector<uint32_t> map_image;
+    int64_t refine_total = 0;
+    for (int i : order) {
+        if (descs[i].level != 9 || descs[i].nblocks == 0) continue;
+        refine_base[i] = refine_total;
+        map_start.push_back(refine_total);
+        map_image.push_back((uint32_t)i);
+        refine_total += descs[i].nblocks;
+    }
+    map_start.push_back(refine_total);
     icbc_gpu_batch *B = new icbc_gpu_batch();
     B->ntasks = (int)tasks.size();
     B->grid = sm_count() * batch_ctas_per_sm();
+    B->refine_total = refine_total;
+    B->map_n = (int)map_image.size();
     cudaError_t e = cudaMalloc(&B->d_images, sizeof(ImageDesc) * std::max(1, n_images));
     if (e == cudaSuccess) e = cudaMalloc(&B->d_tasks, sizeof(BatchTask) * std::max<size_t>(1, tasks.size()));
     if (e == cudaSuccess) e = cudaMalloc(&B->d_counter, sizeof(int));
@@ -423,15 +446,38 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
         e = cudaMemcpy(B->d_images, descs.data(), sizeof(ImageDesc) * n_images, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !tasks.empty())
         e = cudaMemcpy(B->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
-    // Capture "reset the queue counter, run the persistent kernel" once.
+    if (e == cudaSuccess && refine_total) {
+        e = cudaMalloc(&B->d_refine_base, sizeof(int64_t) * n_images);
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_map_start, sizeof(int64_t) * map_start.size());
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_map_image, sizeof(uint32_t) * map_image.size());
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_slots, sizeof(RefineSlot) * (size_t)refine_total);
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_refine_counter, sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(B->d_refine_base, refine_base.data(), sizeof(int64_t) * n_images, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(B->d_map_start, map_start.data(), sizeof(int64_t) * map_start.size(),
+                           cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(B->d_map_image, map_image.data(), sizeof(uint32_t) * map_image.size(),
+                           cudaMemcpyHostToDevice);
+    }
+    // Capture "reset the queue counter, run the persistent kernel" (and the
+    // level-9 refinement pass after it) once.
     cudaStream_t cs = nullptr;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int), cs);
         cudaError_t e2 = e1 == cudaSuccess && B->ntasks
-                             ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter, cs, B->grid)
+                             ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter,
+                                                   cs, B->grid, B->d_refine_base, B->d_slots)
                              : e1;
+        if (e2 == cudaSuccess && refine_total) {
+            e2 = cudaMemsetAsync(B->d_refine_counter, 0, sizeof(unsigned long long), cs);
+            if (e2 == cudaSuccess)
+                e2 = launch_refine_batch(G, B->d_images, RefineMap{B->d_map_start, B->d_map_image, B->map_n},
+                                         B->d_slots, refine_total, B->d_refine_counter, cs, sm_count());
+        }
         e = cudaStreamEndCapture(cs, &B->graph);
         if (e1 != cudaSuccess) e = e1;
         else if (e2 != cudaSuccess) e = e2;
@@ -460,6 +506,11 @@ int icbc_gpu_batch_destroy(icbc_gpu_batch *batch) {
     if (batch->d_images) cudaFree(batch->d_images);
     if (batch->d_tasks) cudaFree(batch->d_tasks);
     if (batch->d_counter) cudaFree(batch->d_counter);
+    if (batch->d_refine_base) cudaFree(batch->d_refine_base);
+    if (batch->d_map_start) cudaFree(batch->d_map_start);
+    if (batch->d_map_image) cudaFree(batch->d_map_image);
+    if (batch->d_slots) cudaFree(batch->d_slots);
+    if (batch->d_refine_counter) cudaFree(batch->d_refine_counter);
     delete batch;
     return ICBC_GPU_OK;
 }

@@ -168,6 +168,46 @@ def test_batch_matches_plain_and_oracle(gpu_lib):
         assert np.array_equal(out.cpu().numpy(), ob)
 
 
+def test_batch_level9_refinement_pass(gpu_lib):
+    """Level-9 images of a batch refine in a second launch whose lanes serve
+    blocks of different images: each image's decoder, flags, colour weights
+    and alpha weights must reach its blocks.  Errors are checked too."""
+    import torch
+    ig = gpu_lib
+    rng = np.random.default_rng(11)
+    cases = []
+    for i in range(24):
+        w, h = int(rng.integers(5, 160)), int(rng.integers(5, 160))
+        level = 9 if i % 4 else int(rng.choice([2, 8]))
+        cases.append(dict(w=w, h=h, level=level, decoder=i % 4, tcm=bool(i % 3), tcb=bool(i % 5),
+                          cw=(1.0, 1.0, 1.0) if i % 2 else (0.299, 0.587, 0.114),
+                          wm=ig.WEIGHTS_ALPHA if i % 3 == 1 else ig.WEIGHTS_UNIFORM, seed=100 + i))
+    imgs, outs, errs, descs = [], [], [], []
+    for c in cases:
+        img = synth.quality_sweep_image(c["w"], c["h"], seed=c["seed"])
+        dev = _to_dev(img)
+        nb = ig.blocks_of(c["w"], c["h"])
+        out = torch.zeros((nb, 8), dtype=torch.uint8, device="cuda")
+        err = torch.zeros(nb, dtype=torch.float32, device="cuda")
+        imgs.append((img, dev))
+        outs.append(out)
+        errs.append(err)
+        descs.append(ig.image_desc(dev, c["level"], out, err, c["decoder"], c["cw"], c["wm"], None, c["tcm"], c["tcb"]))
+    batch = ig.Batch(descs)
+    batch.launch()
+    torch.cuda.synchronize()
+    for (img, dev), c, out, err in zip(imgs, cases, outs, errs):
+        pe = torch.zeros_like(err)
+        po = ig.compress_image(dev, c["level"], c["decoder"], c["cw"], c["wm"], None, c["tcm"], c["tcb"], errors=pe)
+        assert np.array_equal(out.cpu().numpy(), po.cpu().numpy()), c
+        assert same_bits(err.cpu().numpy(), pe.cpu().numpy()), c
+    batch.close()
+    for (img, _), c, out, err in list(zip(imgs, cases, outs, errs))[::3]:
+        ob, oe = O.encode_image(img, c["level"], c["decoder"], c["cw"], c["wm"], None, c["tcm"], c["tcb"], nthreads=8)
+        assert np.array_equal(out.cpu().numpy(), ob), c
+        assert same_bits(err.cpu().numpy(), oe), c
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib
