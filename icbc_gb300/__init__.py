@@ -28,6 +28,8 @@ DECODER_DEFAULT = -1
 Quality_Fast, Quality_Default, Quality_Max = 1, 8, 9
 # weight sources of RGBA8 images
 WEIGHTS_UNIFORM, WEIGHTS_ALPHA, WEIGHTS_PLANE = 0, 1, 2
+# SIMD builds of the reference whose output the *_simd entry points reproduce.
+SIMD_SCALAR, SIMD_SSE2, SIMD_SSE41, SIMD_AVX, SIMD_AVX2, SIMD_AVX512 = 0, 1, 2, 3, 4, 5
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "not initialized", 3: "CUDA error", 4: "out of memory",
           5: "misaligned", 6: "over budget", 7: "not ready", 8: "cancelled", 9: "not found"}
@@ -109,6 +111,8 @@ def load(build_if_missing: bool = True):
             "icbc_gpu_sm_count": (i32, []),
             "icbc_gpu_compress_bc1_blocks": (i32, [i32, vp, vp, f32p, i32, i32, i32, vp, vp, i64, vp]),
             "icbc_gpu_compress_bc1_image": (i32, [ctypes.POINTER(ImageDesc), vp]),
+            "icbc_gpu_compress_bc1_blocks_simd": (i32, [i32, i32, vp, vp, f32p, i32, i32, i32, vp, vp, i64, vp]),
+            "icbc_gpu_compress_bc1_image_simd": (i32, [i32, ctypes.POINTER(ImageDesc), vp]),
             "icbc_gpu_batch_create": (i32, [ctypes.POINTER(ImageDesc), i32, ctypes.POINTER(vp)]),
             "icbc_gpu_batch_launch": (i32, [vp, vp]),
             "icbc_gpu_batch_destroy": (i32, [vp]),
@@ -232,7 +236,7 @@ def debug_tables(decoder: int) -> dict:
 
 def compress_blocks(colors, weights, level: int, decoder: int = DECODER_DEFAULT, color_weights=(1.0, 1.0, 1.0),
                     three_color_mode: bool = True, three_color_black: bool = True, initial=None, stream=None,
-                    out=None, errors=None):
+                    out=None, errors=None, simd_profile: int = 0):
     """Encodes n blocks given as compress_bc1 inputs.
 
     colors: (n,16,4) float32, weights: (n,16) float32 or None (1.0f).  numpy
@@ -240,6 +244,7 @@ def compress_blocks(colors, weights, level: int, decoder: int = DECODER_DEFAULT,
     tensors stay on the device and (blocks uint8 (n,8), errors float32 (n,))
     tensors are returned.  ``initial`` seeds the output bytes (kept by levels
     4..9 when no candidate has a finite error, as the reference does).
+    ``simd_profile`` (SIMD_*) reproduces a SIMD build of the reference.
     """
     torch = _torch()
     L = load()
@@ -259,9 +264,12 @@ def compress_blocks(colors, weights, level: int, decoder: int = DECODER_DEFAULT,
     if errors is None:
         errors = torch.empty(n, dtype=torch.float32, device=dev)
     cw = _cw(color_weights)
-    st = L.icbc_gpu_compress_bc1_blocks(int(level), c.data_ptr(), None if w is None else w.data_ptr(), cw,
-                                        int(bool(three_color_mode)), int(bool(three_color_black)), int(decoder),
-                                        out.data_ptr(), errors.data_ptr(), n, _stream_ptr(stream))
+    args = (int(level), c.data_ptr(), None if w is None else w.data_ptr(), cw, int(bool(three_color_mode)),
+            int(bool(three_color_black)), int(decoder), out.data_ptr(), errors.data_ptr(), n, _stream_ptr(stream))
+    if simd_profile:
+        st = L.icbc_gpu_compress_bc1_blocks_simd(int(simd_profile), *args)
+    else:
+        st = L.icbc_gpu_compress_bc1_blocks(*args)
     _check(st, "compress_bc1_blocks")
     if on_host:
         torch.cuda.current_stream().synchronize() if stream is None else stream.synchronize()
@@ -298,8 +306,10 @@ def blocks_of(width: int, height: int) -> int:
 
 def compress_image(rgba, level: int, decoder: int = DECODER_DEFAULT, color_weights=(1.0, 1.0, 1.0),
                    weight_mode: int = WEIGHTS_UNIFORM, weight_plane=None, three_color_mode: bool = True,
-                   three_color_black: bool = True, out=None, errors=None, with_errors: bool = False, stream=None):
-    """Plain form: one launch for one RGBA8 image (CUDA uint8 tensor (h,w,4))."""
+                   three_color_black: bool = True, out=None, errors=None, with_errors: bool = False, stream=None,
+                   simd_profile: int = 0):
+    """Plain form: one launch for one RGBA8 image (CUDA uint8 tensor (h,w,4)).
+    ``simd_profile`` (SIMD_*) reproduces a SIMD build of the reference."""
     torch = _torch()
     L = load()
     h, w = int(rgba.shape[0]), int(rgba.shape[1])
@@ -310,7 +320,11 @@ def compress_image(rgba, level: int, decoder: int = DECODER_DEFAULT, color_weigh
         errors = torch.empty(nb, dtype=torch.float32, device=rgba.device)
     d = image_desc(rgba, level, out, errors, decoder, color_weights, weight_mode, weight_plane, three_color_mode,
                    three_color_black)
-    _check(L.icbc_gpu_compress_bc1_image(ctypes.byref(d), _stream_ptr(stream)), "compress_bc1_image")
+    if simd_profile:
+        st = L.icbc_gpu_compress_bc1_image_simd(int(simd_profile), ctypes.byref(d), _stream_ptr(stream))
+    else:
+        st = L.icbc_gpu_compress_bc1_image(ctypes.byref(d), _stream_ptr(stream))
+    _check(st, "compress_bc1_image")
     return (out, errors) if with_errors else out
 
 

@@ -35,11 +35,14 @@ def nvcc() -> str:
 
 def _units():
     """(source, extra flags, object name) of every translation unit."""
-    units = [(os.path.join(CSRC, "bc1_level.cu"), ["-DICBC_LEVEL=%d" % lv], "bc1_level%d.o" % lv)
-             for lv in range(10)]
+    # The all-levels units (batch, SIMD profiles, no-alloc) compile longest: start them first.
+    units = [(os.path.join(CSRC, n), [], n.replace(".cu", ".o"))
+             for n in ("bc1_batch.cu", "bc1_simd.cu", "bc1_noalloc.cu")]
+    units += [(os.path.join(CSRC, "bc1_level.cu"), ["-DICBC_LEVEL=%d" % lv], "bc1_level%d.o" % lv)
+              for lv in range(9, -1, -1)]
     units += [(os.path.join(CSRC, n), [], n.replace(".cu", ".o"))
-              for n in ("bc1_batch.cu", "bc1_decode.cu", "icbc_gpu_api.cu", "icbc_gpu_serve.cu",
-                        "icbc_compat.cu", "bc1_noalloc.cu", "bc1_refine.cu", "icbc_containers.cu")]
+              for n in ("bc1_decode.cu", "icbc_gpu_api.cu", "icbc_gpu_serve.cu", "icbc_compat.cu", "bc1_refine.cu",
+                        "icbc_containers.cu")]
     return [u for u in units if os.path.exists(u[0])]
 
 

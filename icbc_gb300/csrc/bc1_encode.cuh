@@ -62,6 +62,10 @@ struct EncodeParams {
     int three_color_mode;
     int three_color_black;
     V3 cw;
+    // SIMD profile of the reference build reproduced by the profile kernels
+    // (bc1_simd.cu): vector width of the cluster loops, fused vmadd/vmsub,
+    // vround01 half to even.  The plain kernels ignore these.
+    int simd_vec, simd_fma, simd_rne;
 };
 
 // Everything one warp needs for a group of 32 blocks.
@@ -529,6 +533,115 @@ __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, cons
     return dot(e1, q.metric);
 }
 
+// ----------------------------------------------- SIMD-profile cluster fit --
+//
+// The reference's SIMD builds (ICBC_SIMD 1..5, icbc.h:427-1369) run the same
+// cluster loops with vmadd / vmsub fused on AVX2 and AVX-512 (icbc.h:734-752,
+// :970-976) and vround01 rounding half to even from SSE4.1 on (icbc.h:518-524,
+// :764-766, :988-990).  These are cf4_combo / cf3_combo with those two choices.
+__device__ __forceinline__ float pm_madd(bool f, float a, float b, float c) {
+    return f ? __fmaf_rn(a, b, c) : a * b + c;
+}
+__device__ __forceinline__ float pm_msub(bool f, float a, float b, float c) {
+    return f ? __fmaf_rn(a, b, -c) : a * b - c;
+}
+// vm2sub(a, b, c, d) = vmsub(a, b, c * d) (icbc.h:415, :754-756, :978-980).
+__device__ __forceinline__ float pm_m2sub(bool f, float a, float b, float c, float d) { return pm_msub(f, a, b, c * d); }
+// vround5 / vround6 of a saturated value: int(t + 0.5f) or round-half-even
+// of t = x * n, both exact for 0 <= t < 2^23 through the 2^23 addition.
+__device__ __forceinline__ float pm_round(float x, float n, float inv_n, bool rne) {
+    const float t = __saturatef(x) * n;
+    const float r = rne ? __fsub_rn(__fadd_rn(t, 8388608.0f), 8388608.0f) : snap_floor(t + 0.5f);
+    return r * inv_n;
+}
+__device__ __forceinline__ V3 pm_round_ept(V3 v, bool rne) {
+    return v3(pm_round(v.x, 31.0f, 1.0f / 31.0f, rne), pm_round(v.y, 63.0f, 1.0f / 63.0f, rne),
+              pm_round(v.z, 31.0f, 1.0f / 31.0f, rne));
+}
+
+// cluster_fit_four's iteration (icbc.h:2685-2733) under a SIMD profile.
+__device__ __forceinline__ float cf4_combo_simd(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
+                                               bool f, bool rne, V3 &a, V3 &b) {
+    const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
+    V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
+    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
+    V3 x2 = v3(S[i2], S[17 + i2], S[34 + i2]);
+    const float w0 = S[51 + i0];
+    float w1 = S[51 + i1], w2 = S[51 + i2];
+    const float w3 = k.w_sum - w2;
+    x2 = x2 - x1;
+    x1 = x1 - x0;
+    w2 = w2 - w1;
+    w1 = w1 - w0;
+    const float alpha2 = pm_madd(f, w2, q.w1_9, pm_madd(f, w1, q.w4_9, w0));
+    const float beta2 = pm_madd(f, w1, q.w1_9, pm_madd(f, w2, q.w4_9, w3));
+    const float ab = (w1 + w2) * q.w2_9;
+    const float factor = 1.0f / pm_m2sub(f, alpha2, beta2, ab, ab);
+    const V3 ax = v3(pm_madd(f, x2.x, q.w1_3, pm_madd(f, x1.x, q.w2_3, x0.x)),
+                     pm_madd(f, x2.y, q.w1_3, pm_madd(f, x1.y, q.w2_3, x0.y)),
+                     pm_madd(f, x2.z, q.w1_3, pm_madd(f, x1.z, q.w2_3, x0.z)));
+    const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
+    a = pm_round_ept(v3(pm_m2sub(f, ax.x, beta2, bx.x, ab) * factor, pm_m2sub(f, ax.y, beta2, bx.y, ab) * factor,
+                        pm_m2sub(f, ax.z, beta2, bx.z, ab) * factor), rne);
+    b = pm_round_ept(v3(pm_m2sub(f, bx.x, alpha2, ax.x, ab) * factor, pm_m2sub(f, bx.y, alpha2, ax.y, ab) * factor,
+                        pm_m2sub(f, bx.z, alpha2, ax.z, ab) * factor), rne);
+    const V3 e2 = v3(pm_m2sub(f, a.x, pm_msub(f, b.x, ab, ax.x), b.x, bx.x) * 2.0f,
+                     pm_m2sub(f, a.y, pm_msub(f, b.y, ab, ax.y), b.y, bx.y) * 2.0f,
+                     pm_m2sub(f, a.z, pm_msub(f, b.z, ab, ax.z), b.z, bx.z) * 2.0f);
+    const V3 e1 = v3(pm_madd(f, a.x * a.x, alpha2, pm_madd(f, b.x * b.x, beta2, e2.x)),
+                     pm_madd(f, a.y * a.y, alpha2, pm_madd(f, b.y * b.y, beta2, e2.y)),
+                     pm_madd(f, a.z * a.z, alpha2, pm_madd(f, b.z * b.z, beta2, e2.z)));
+    return dot(e1, q.metric);
+}
+
+// cluster_fit_three's iteration (icbc.h:2299-2323) under a SIMD profile.
+__device__ __forceinline__ float cf3_combo_simd(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
+                                               bool f, bool rne, V3 &a, V3 &b) {
+    const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
+    const V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
+    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
+    const float w0 = S[51 + i0];
+    float w1 = S[51 + i1];
+    const float w2 = k.w_sum - w1;
+    x1 = x1 - x0;
+    w1 = w1 - w0;
+    const float ab = w1 * 0.25f;
+    const float alpha2 = w0 + ab;
+    const float beta2 = w2 + ab;
+    const float factor = 1.0f / pm_m2sub(f, alpha2, beta2, ab, ab);
+    const V3 ax = x0 + x1 * 0.5f;
+    const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
+    a = pm_round_ept(v3(pm_m2sub(f, ax.x, beta2, bx.x, ab) * factor, pm_m2sub(f, ax.y, beta2, bx.y, ab) * factor,
+                        pm_m2sub(f, ax.z, beta2, bx.z, ab) * factor), rne);
+    b = pm_round_ept(v3(pm_m2sub(f, bx.x, alpha2, ax.x, ab) * factor, pm_m2sub(f, bx.y, alpha2, ax.y, ab) * factor,
+                        pm_m2sub(f, bx.z, alpha2, ax.z, ab) * factor), rne);
+    const V3 e2 = v3(pm_m2sub(f, a.x, pm_msub(f, b.x, ab, ax.x), b.x, bx.x) * 2.0f,
+                     pm_m2sub(f, a.y, pm_msub(f, b.y, ab, ax.y), b.y, bx.y) * 2.0f,
+                     pm_m2sub(f, a.z, pm_msub(f, b.z, ab, ax.z), b.z, bx.z) * 2.0f);
+    const V3 e1 = v3(pm_madd(f, a.x * a.x, alpha2, pm_madd(f, b.x * b.x, beta2, e2.x)),
+                     pm_madd(f, a.y * a.y, alpha2, pm_madd(f, b.y * b.y, beta2, e2.y)),
+                     pm_madd(f, a.z * a.z, alpha2, pm_madd(f, b.z * b.z, beta2, e2.z)));
+    return dot(e1, q.metric);
+}
+
+// compute_sat's FLT_MAX fill of the entries past the colour count
+// (icbc.h:1931-1936), which the SIMD loops read for their padding lanes.
+__device__ __forceinline__ void fill_sat_tail(float *srow, int m) {
+    for (int k = m + 1; k <= 16; k++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) srow[c * 17 + k] = FLT_MAX;
+    }
+}
+
+// In a SIMD build, combination k of a block is evaluated in lane k % vec;
+// each lane keeps its first strict minimum and the cross-lane reduction
+// (reduce_min_index, icbc.h:574-586, :812-831, :1031-1039) takes the smallest
+// error, ties to the lowest lane.  So the winner is the smallest
+// (error, k % vec, k / vec); the rank below orders the last two.
+// vec is a power of two (1, 4, 8 or 16).
+__device__ __forceinline__ int simd_rank(int k, int vec) { return ((k & (vec - 1)) << 10) | (k >> (__ffs(vec) - 1)); }
+__device__ __forceinline__ int simd_unrank(int r, int vec) { return (r & 1023) * vec + (r >> 10); }
+
 // Warp-cooperative search of the cluster combinations of every block of the
 // warp that needs one.  The warp's whole work -- the concatenation of each
 // block's combination list -- is cut into 64 equal contiguous ranges; lane l
@@ -550,14 +663,20 @@ struct Walker {
 
 __device__ __forceinline__ int block_info(const WarpCtx &w, int b) { return __float_as_int(w.sat[b * kSatStride + 68]); }
 
-template <bool FOUR>
-__device__ __forceinline__ void walker_enter(const WarpCtx &w, Walker &v, int b, int k) {
+// With SIMD, a block's combinations run to a whole number of vectors of
+// `vec` lanes (icbc.h:2089, :2362: the padding lanes read table entries of
+// larger counts, or zeros, against the SAT's FLT_MAX fill).
+__device__ __forceinline__ int padded_total(int t, int vec) { return (t + vec - 1) / vec * vec; }
+
+template <bool FOUR, bool SIMD = false>
+__device__ __forceinline__ void walker_enter(const WarpCtx &w, Walker &v, int b, int k, int vec = 1) {
     const float *S = w.sat + b * kSatStride;
     const int cnt = __float_as_int(S[68]) >> 16;
     v.b = b;
     v.k = k;
     v.S = S;
     v.total = FOUR ? w.T->four_total[cnt - 1] : w.T->three_total[cnt - 1];
+    if (SIMD) v.total = padded_total(v.total, vec);
     v.sums = fit_sums(S, cnt);
     v.best = FLT_MAX;
     v.best_k = 0x7fffffff;
@@ -573,8 +692,8 @@ __device__ __forceinline__ void walker_flush(const WarpCtx &w, const Walker &v) 
 }
 
 // Starts a walker at global combination g (if any work is left for it).
-template <bool FOUR>
-__device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g, int gend) {
+template <bool FOUR, bool SIMD = false>
+__device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g, int gend, int vec = 1) {
     v.g = g;
     v.gend = gend;
     v.S = w.sat;
@@ -592,7 +711,7 @@ __device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g,
             if ((block_info(w, mid) & 0xffff) <= g) lo = mid;
             else hi = mid;
         }
-        walker_enter<FOUR>(w, v, lo, g - (block_info(w, lo) & 0xffff));
+        walker_enter<FOUR, SIMD>(w, v, lo, g - (block_info(w, lo) & 0xffff), vec);
     }
 }
 
@@ -600,29 +719,41 @@ __device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g,
 // into the next block with work when this one is done.  `next` is the table
 // entry of the following combination, loaded one iteration ahead; a block
 // change reloads it.
-template <bool FOUR>
-__device__ __forceinline__ void walker_step(const WarpCtx &w, Walker &v, float e, uint32_t &next) {
+// With SIMD the walker keeps the smallest (error, simd_rank) of its share
+// in best / best_k (best_k holds the rank), never an error of FLT_MAX.
+template <bool FOUR, bool SIMD = false>
+__device__ __forceinline__ void walker_step(const WarpCtx &w, Walker &v, float e, uint32_t &next, int vec = 1) {
     const bool live = v.g < v.gend;
-    const bool better = live && e < v.best;
+    bool better;
+    int rk = v.k;
+    if (SIMD) {
+        rk = simd_rank(v.k, vec);
+        better = live && (e < v.best || (e == v.best && v.best_k != 0x7fffffff && rk < v.best_k));
+    } else {
+        better = live && e < v.best;
+    }
     v.best = better ? e : v.best;
-    v.best_k = better ? v.k : v.best_k;
+    v.best_k = better ? rk : v.best_k;
     v.g += live;
     v.k += live;
     if (live && v.k == v.total && v.g < v.gend) {
         walker_flush(w, v);
         int nb = v.b + 1;
         while ((block_info(w, nb) >> 16) == 0) nb++;
-        walker_enter<FOUR>(w, v, nb, 0);
+        walker_enter<FOUR, SIMD>(w, v, nb, 0, vec);
         next = (FOUR ? w.T->four : w.T->three)[0];
     }
 }
 
 // Returns this lane's winning table index, or -1 (no search, or no error
 // below FLT_MAX: the reference then keeps zero endpoints).
-template <bool FOUR>
-__device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int count, const FitWeights &q) {
+template <bool FOUR, bool SIMD = false>
+__device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int count, const FitWeights &q,
+                                           const EncodeParams *p = nullptr) {
     const int lane = w.lane;
-    const int T = need ? (FOUR ? w.T->four_total[count - 1] : w.T->three_total[count - 1]) : 0;
+    const int vec = SIMD ? p->simd_vec : 1;
+    int T = need ? (FOUR ? w.T->four_total[count - 1] : w.T->three_total[count - 1]) : 0;
+    if (SIMD) T = padded_total(T, vec);
     int incl = T;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -636,19 +767,29 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
     if (W == 0) return -1;
     const int per = (W + 63) / 64;
     Walker A, B;
-    walker_start<FOUR>(w, A, min(lane * per, W), min(lane * per + per, W));
-    walker_start<FOUR>(w, B, min((lane + 32) * per, W), min((lane + 32) * per + per, W));
+    walker_start<FOUR, SIMD>(w, A, min(lane * per, W), min(lane * per + per, W), vec);
+    walker_start<FOUR, SIMD>(w, B, min((lane + 32) * per, W), min((lane + 32) * per + per, W), vec);
     const uint32_t *table = FOUR ? w.T->four : w.T->three;
+    // The padded SIMD range reaches the last table entry; its look-ahead
+    // index is clamped to the table (that entry is then never used).
+    const int last = FOUR ? 991 : 159;
     uint32_t pa = table[A.k], pb = table[B.k];
     for (int it = 0; it < per; it++) {
         // Entry k + 1 of each walker is fetched before this step's arithmetic
         // (the tables are padded past their last used entry).
-        uint32_t na = table[A.k + 1], nb = table[B.k + 1];
+        uint32_t na = table[SIMD ? min(A.k + 1, last) : A.k + 1], nb = table[SIMD ? min(B.k + 1, last) : B.k + 1];
         V3 a, b;
-        const float ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
-        const float eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
-        walker_step<FOUR>(w, A, ea, na);
-        walker_step<FOUR>(w, B, eb, nb);
+        float ea, eb;
+        if (SIMD) {
+            const bool f = p->simd_fma != 0, rne = p->simd_rne != 0;
+            ea = FOUR ? cf4_combo_simd(A.S, pa, A.sums, q, f, rne, a, b) : cf3_combo_simd(A.S, pa, A.sums, q, f, rne, a, b);
+            eb = FOUR ? cf4_combo_simd(B.S, pb, B.sums, q, f, rne, a, b) : cf3_combo_simd(B.S, pb, B.sums, q, f, rne, a, b);
+        } else {
+            ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
+            eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
+        }
+        walker_step<FOUR, SIMD>(w, A, ea, na, vec);
+        walker_step<FOUR, SIMD>(w, B, eb, nb, vec);
         pa = na;
         pb = nb;
     }
@@ -656,7 +797,8 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
     walker_flush(w, B);
     __syncwarp();
     const unsigned long long key = w.slots[lane];
-    return (need && key != ~0ull) ? (int)(uint32_t)key : -1;
+    if (!need || key == ~0ull) return -1;
+    return SIMD ? simd_unrank((int)(uint32_t)key, vec) : (int)(uint32_t)key;
 }
 
 // ------------------------------------------------------------- encoder --
@@ -669,7 +811,7 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 // With DEFER the refinement of level 9 is not run here: `refine_next` is set
 // for the blocks it applies to (the caller hands them to k_refine), and the
 // returned error is the one refinement starts from.
-template <int L, bool DEFER>
+template <int L, bool DEFER, bool SIMD = false>
 __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
                                                 uint32_t &c1, uint32_t &idx, bool &refine_next) {
     using O = Level<L>;
@@ -704,6 +846,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
             }
             if (O::cluster) {
                 build_sat_inplace(srow, count, false);
+                if (SIMD) fill_sat_tail(srow, count);
                 need4 = true;
             }
         }
@@ -714,14 +857,17 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
         __syncwarp();
         // 4-colour cluster fit of every block that needs one, across the warp.
         const FitWeights q = fit_weights(w.D, metric);
-        const int my4 = flat_search<true>(w, need4, count, q);
+        const int my4 = flat_search<true, SIMD>(w, need4, count, q, &p);
         uint32_t f0 = 0, f1 = 0, fi = 0;
         float ferr = 0.0f;
         bool need3 = false;
         int count3 = count;
         if (need4) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
-            if (my4 >= 0) cf4_combo(srow, w.T->four[my4], fit_sums(srow, count), q, a, b);
+            if (my4 >= 0) {
+                if (SIMD) cf4_combo_simd(srow, w.T->four[my4], fit_sums(srow, count), q, p.simd_fma, p.simd_rne, a, b);
+                else cf4_combo(srow, w.T->four[my4], fit_sums(srow, count), q, a, b);
+            }
             ferr = output_block4(w, row, p, a, b, f0, f1, fi);
             const bool use_black = any_black && p.three_color_black;
             const bool use_three = (O::cf3_always && p.three_color_mode) ||
@@ -733,6 +879,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
                     bool ab;
                     reduce_colors(row, O::threshold, srow, ab);
                     count3 = build_sat_inplace(srow, count, true);
+                    if (SIMD) fill_sat_tail(srow, count3);
                     need3 = count3 > 0;
                 } else {
                     need3 = true;
@@ -740,10 +887,13 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
             }
         }
         __syncwarp();
-        const int my3 = flat_search<false>(w, need3, count3, q);
+        const int my3 = flat_search<false, SIMD>(w, need3, count3, q, &p);
         if (need3) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
-            if (my3 >= 0) cf3_combo(srow, w.T->three[my3], fit_sums(srow, count3), q, a, b);
+            if (my3 >= 0) {
+                if (SIMD) cf3_combo_simd(srow, w.T->three[my3], fit_sums(srow, count3), q, p.simd_fma, p.simd_rne, a, b);
+                else cf3_combo(srow, w.T->three[my3], fit_sums(srow, count3), q, a, b);
+            }
             uint32_t t0, t1, ti;
             const float e3 = output_block3(w, row, p, a, b, t0, t1, ti);
             if (e3 < ferr) { ferr = e3; f0 = t0; f1 = t1; fi = ti; }

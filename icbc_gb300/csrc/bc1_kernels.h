@@ -41,11 +41,15 @@ struct BatchTask {
 using BlocksLauncher = cudaError_t (*)(const GlobalTables *, const BlocksSrc &, const EncodeParams &, void *, float *,
                                        int64_t, cudaStream_t, int);
 using ImageLauncher = cudaError_t (*)(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t, int);
+using ImageLauncherExt = cudaError_t (*)(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t,
+                                         int, RefineSlot *, unsigned long long *);
 
 #define ICBC_DECLARE_LEVEL(L)                                                                                    \
     cudaError_t launch_blocks_l##L(const GlobalTables *, const BlocksSrc &, const EncodeParams &, void *, float *, \
                                    int64_t, cudaStream_t, int);                                                  \
-    cudaError_t launch_image_l##L(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t, int);
+    cudaError_t launch_image_l##L(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t, int); \
+    cudaError_t launch_image_ext_l##L(const GlobalTables *, const ImageDesc &, const EncodeParams &, cudaStream_t, int, \
+                                      RefineSlot *, unsigned long long *);
 ICBC_DECLARE_LEVEL(0)
 ICBC_DECLARE_LEVEL(1)
 ICBC_DECLARE_LEVEL(2)
@@ -88,6 +92,11 @@ struct RefineMap {
 cudaError_t launch_refine_batch(const GlobalTables *G, const ImageDesc *images, RefineMap map,
                                 const RefineSlot *slots, int64_t total, unsigned long long *counter,
                                 cudaStream_t stream, int sms);
+
+// The SIMD-profile encoder (bc1_simd.cu), levels 2..9: an image (`image`)
+// or float blocks (`blocks`), p.simd_* set.
+cudaError_t launch_simd(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks, const EncodeParams &p,
+                        uint2 *out, float *errors, int64_t n, int level, cudaStream_t stream);
 
 // Launch shape of the plain kernels of a level (autotuned or default).
 struct LaunchShape {

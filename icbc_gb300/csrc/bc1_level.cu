@@ -122,10 +122,14 @@ static int grid_for(K kernel, int64_t n, int sms) {
 // scratch.  Other levels are one launch.
 constexpr bool kDefer = Level<L>::refine;
 
+// The level-9 hand-over lives in stream-ordered scratch, or in the caller's
+// `ext_st` (n slots) and `ext_counter` when given (graph captures, where
+// nothing is allocated).
 template <class Kernel, class Launch>
 static cudaError_t run(Kernel kernel, int64_t n, int sms, cudaStream_t stream, Launch launch,
                        const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks, const EncodeParams &p,
-                       uint2 *out, float *errors) {
+                       uint2 *out, float *errors, RefineSlot *ext_st = nullptr,
+                       unsigned long long *ext_counter = nullptr) {
     const size_t smem = smem_bytes(Level<L>::cluster);
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -134,18 +138,23 @@ static cudaError_t run(Kernel kernel, int64_t n, int sms, cudaStream_t stream, L
         launch(grid, smem, nullptr);
         return cudaGetLastError();
     }
-    const size_t slots = ((size_t)n * sizeof(RefineSlot) + 15) / 16 * 16;
     void *scratch = nullptr;
-    e = scratch_alloc(&scratch, slots + 16, stream);
-    if (e != cudaSuccess) return e;
-    RefineSlot *st = reinterpret_cast<RefineSlot *>(scratch);
-    unsigned long long *counter = reinterpret_cast<unsigned long long *>(static_cast<char *>(scratch) + slots);
+    RefineSlot *st = ext_st;
+    unsigned long long *counter = ext_counter;
+    if (!st) {
+        const size_t slots = ((size_t)n * sizeof(RefineSlot) + 15) / 16 * 16;
+        e = scratch_alloc(&scratch, slots + 16, stream);
+        if (e != cudaSuccess) return e;
+        st = reinterpret_cast<RefineSlot *>(scratch);
+        counter = reinterpret_cast<unsigned long long *>(static_cast<char *>(scratch) + slots);
+    }
     e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
     if (e == cudaSuccess) {
         launch(grid, smem, st);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = launch_refine(G, image, blocks, p, out, errors, st, n, counter, stream, sms);
+    if (!scratch) return e;
     const cudaError_t f = scratch_free(scratch, stream);
     return e != cudaSuccess ? e : f;
 }
@@ -167,6 +176,18 @@ cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const Im
                    k_encode_image<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, st);
                },
                G, &d, nullptr, p, d.out, d.errors);
+}
+
+// As launch_image_l<L>, with level 9's hand-over in the caller's memory
+// (d.nblocks slots and a counter; unused at the other levels).
+cudaError_t ICBC_CAT(launch_image_ext_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
+                                                     cudaStream_t stream, int sms, RefineSlot *st,
+                                                     unsigned long long *counter) {
+    return run(k_encode_image<L, kDefer>, d.nblocks, sms, stream,
+               [&](int grid, size_t smem, RefineSlot *slots) {
+                   k_encode_image<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, slots);
+               },
+               G, &d, nullptr, p, d.out, d.errors, st, counter);
 }
 
 }  // namespace icbc_gpu

@@ -154,6 +154,16 @@ const BlocksLauncher kBlocksLaunch[10] = {launch_blocks_l0, launch_blocks_l1, la
 const ImageLauncher kImageLaunch[10] = {launch_image_l0, launch_image_l1, launch_image_l2, launch_image_l3,
                                         launch_image_l4, launch_image_l5, launch_image_l6, launch_image_l7,
                                         launch_image_l8, launch_image_l9};
+const ImageLauncherExt kImageLaunchExt[10] = {launch_image_ext_l0, launch_image_ext_l1, launch_image_ext_l2,
+                                              launch_image_ext_l3, launch_image_ext_l4, launch_image_ext_l5,
+                                              launch_image_ext_l6, launch_image_ext_l7, launch_image_ext_l8,
+                                              launch_image_ext_l9};
+
+// An image of at least this many blocks (a 4096 x 4096 image) fills the GPU
+// for many waves on its own: inside a batch it gets its level's own kernel,
+// whose code is one level's, rather than a share of the all-levels batch
+// kernel, which gains it nothing and fetches instructions from a larger body.
+constexpr int64_t kOwnLaunchBlocks = int64_t(1) << 20;
 
 int sm_count() {
     static int sms[64] = {};
@@ -186,8 +196,18 @@ EncodeParams make_params(int decoder, int tc, int tcb, const float cw[3]) {
     p.three_color_mode = tc ? 1 : 0;
     p.three_color_black = tcb ? 1 : 0;
     p.cw = V3{cw[0], cw[1], cw[2]};
+    p.simd_vec = 1;
+    p.simd_fma = 0;
+    p.simd_rne = 0;
     return p;
 }
+
+// Cluster-loop parameters of the reference's SIMD builds (ICBC_SIMD 0..5,
+// icbc.h:59-64): vector width, fused vmadd/vmsub, vround01 half to even.
+struct SimdProfile {
+    int vec, fma, rne;
+};
+constexpr SimdProfile kSimdProfiles[6] = {{1, 0, 0}, {4, 0, 0}, {4, 0, 1}, {8, 0, 1}, {8, 1, 1}, {16, 1, 1}};
 
 // Validates an image descriptor and resolves it for the kernels.
 int resolve_image(const icbc_gpu_image &im, ImageDesc &d) {
@@ -383,6 +403,55 @@ int icbc_gpu_compress_bc1_blocks(int level, const float *d_colors, const float *
     return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
 }
 
+int icbc_gpu_compress_bc1_blocks_simd(int simd_profile, int level, const float *d_colors, const float *d_weights,
+                                      const float color_weights[3], int three_color_mode, int three_color_black,
+                                      int decoder, void *d_out, float *d_errors, int64_t n_blocks, void *stream) {
+    if (simd_profile < 0 || simd_profile > 5) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    // The scalar profile, and levels without a cluster fit, are the plain path.
+    if (simd_profile == 0 || level == 0 || level == 1)
+        return icbc_gpu_compress_bc1_blocks(level, d_colors, d_weights, color_weights, three_color_mode,
+                                            three_color_black, decoder, d_out, d_errors, n_blocks, stream);
+    if (level < 0 || level > 9 || n_blocks < 0 || !color_weights) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (n_blocks == 0) return ICBC_GPU_OK;
+    if (!d_colors || !d_out) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(d_colors, 16) || (d_weights && !aligned(d_weights, 16)) || !aligned(d_out, 8) ||
+        (d_errors && !aligned(d_errors, 4)))
+        return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(decoder, &dec);
+    if (st) return st;
+    const GlobalTables *G = nullptr;
+    st = ensure_device_tables(&G);
+    if (st) return st;
+    EncodeParams p = make_params(dec, three_color_mode, three_color_black, color_weights);
+    p.simd_vec = kSimdProfiles[simd_profile].vec;
+    p.simd_fma = kSimdProfiles[simd_profile].fma;
+    p.simd_rne = kSimdProfiles[simd_profile].rne;
+    BlocksSrc src{d_colors, d_weights};
+    cudaError_t e = launch_simd(G, nullptr, &src, p, reinterpret_cast<uint2 *>(d_out), d_errors, n_blocks, level,
+                                reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+int icbc_gpu_compress_bc1_image_simd(int simd_profile, const icbc_gpu_image *image, void *stream) {
+    if (simd_profile < 0 || simd_profile > 5 || !image) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (simd_profile == 0 || image->level == 0 || image->level == 1) return icbc_gpu_compress_bc1_image(image, stream);
+    ImageDesc d;
+    int st = resolve_image(*image, d);
+    if (st) return st;
+    const GlobalTables *G = nullptr;
+    st = ensure_device_tables(&G);
+    if (st) return st;
+    if (d.nblocks == 0) return ICBC_GPU_OK;
+    EncodeParams p = make_params(d.decoder, d.three_color_mode, d.three_color_black, d.cw);
+    p.simd_vec = kSimdProfiles[simd_profile].vec;
+    p.simd_fma = kSimdProfiles[simd_profile].fma;
+    p.simd_rne = kSimdProfiles[simd_profile].rne;
+    cudaError_t e = launch_simd(G, &d, nullptr, p, d.out, d.errors, d.nblocks, d.level,
+                                reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
 int icbc_gpu_compress_bc1_image(const icbc_gpu_image *image, void *stream) {
     if (!image) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     ImageDesc d;
@@ -418,22 +487,34 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
             return kLevelCost[descs[a].level] > kLevelCost[descs[b].level];
         return descs[a].nblocks > descs[b].nblocks;
     });
+    std::vector<int> own;  // images that get their level's own launch
     std::vector<BatchTask> tasks;
-    for (int i : order)
+    for (int i : order) {
+        if (descs[i].nblocks >= kOwnLaunchBlocks) {
+            own.push_back(i);
+            continue;
+        }
         for (int64_t b = 0; b < descs[i].nblocks; b += 32) tasks.push_back(BatchTask{(uint32_t)i, (uint32_t)b});
+    }
     if (tasks.size() > 0x7fffffff) return ICBC_GPU_ERR_INVALID_ARGUMENT;
-    // Refinement slots of the level-9 images, in task order.
-    std::vector<int64_t> refine_base((size_t)n_images, -1), map_start;
+    // Refinement slots of the level-9 images, in task order; then those of
+    // the level-9 images with their own launch, one counter each.
+    std::vector<int64_t> refine_base((size_t)n_images, -1), map_start, own_base;
     std::vector<uint32_t> map_image;
     int64_t refine_total = 0;
     for (int i : order) {
-        if (descs[i].level != 9 || descs[i].nblocks == 0) continue;
+        if (descs[i].level != 9 || descs[i].nblocks == 0 || descs[i].nblocks >= kOwnLaunchBlocks) continue;
         refine_base[i] = refine_total;
         map_start.push_back(refine_total);
         map_image.push_back((uint32_t)i);
         refine_total += descs[i].nblocks;
     }
     map_start.push_back(refine_total);
+    int64_t slots_total = refine_total;
+    for (int i : own) {
+        own_base.push_back(descs[i].level == 9 ? slots_total : -1);
+        if (descs[i].level == 9) slots_total += descs[i].nblocks;
+    }
     icbc_gpu_batch *B = new icbc_gpu_batch();
     B->ntasks = (int)tasks.size();
     B->grid = sm_count() * batch_ctas_per_sm();
@@ -446,12 +527,15 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
         e = cudaMemcpy(B->d_images, descs.data(), sizeof(ImageDesc) * n_images, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !tasks.empty())
         e = cudaMemcpy(B->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && slots_total) {
+        e = cudaMalloc(&B->d_slots, sizeof(RefineSlot) * (size_t)slots_total);
+        // counter 0: the batch's refinement queue; 1..: one per own-launch image
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_refine_counter, sizeof(unsigned long long) * (1 + own.size()));
+    }
     if (e == cudaSuccess && refine_total) {
         e = cudaMalloc(&B->d_refine_base, sizeof(int64_t) * n_images);
         if (e == cudaSuccess) e = cudaMalloc(&B->d_map_start, sizeof(int64_t) * map_start.size());
         if (e == cudaSuccess) e = cudaMalloc(&B->d_map_image, sizeof(uint32_t) * map_image.size());
-        if (e == cudaSuccess) e = cudaMalloc(&B->d_slots, sizeof(RefineSlot) * (size_t)refine_total);
-        if (e == cudaSuccess) e = cudaMalloc(&B->d_refine_counter, sizeof(unsigned long long));
         if (e == cudaSuccess)
             e = cudaMemcpy(B->d_refine_base, refine_base.data(), sizeof(int64_t) * n_images, cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
@@ -477,6 +561,13 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
             if (e2 == cudaSuccess)
                 e2 = launch_refine_batch(G, B->d_images, RefineMap{B->d_map_start, B->d_map_image, B->map_n},
                                          B->d_slots, refine_total, B->d_refine_counter, cs, sm_count());
+        }
+        for (size_t j = 0; j < own.size() && e2 == cudaSuccess; j++) {
+            const ImageDesc &d = descs[own[j]];
+            RefineSlot *st = own_base[j] >= 0 ? B->d_slots + own_base[j] : nullptr;
+            unsigned long long *counter = own_base[j] >= 0 ? B->d_refine_counter + 1 + j : nullptr;
+            e2 = kImageLaunchExt[d.level](G, d, make_params(d.decoder, d.three_color_mode, d.three_color_black, d.cw),
+                                          cs, sm_count(), st, counter);
         }
         e = cudaStreamEndCapture(cs, &B->graph);
         if (e1 != cudaSuccess) e = e1;

@@ -114,6 +114,35 @@ typedef struct icbc_gpu_image {
  * 1.0f, as icbc_test.cpp:398-406 does before calling compress_bc1. */
 int icbc_gpu_compress_bc1_image(const icbc_gpu_image *image, void *stream);
 
+/* ------------------------------------------------------------------------
+ * SIMD profiles.  The reference gives slightly different blocks depending on
+ * the SIMD backend it was compiled with (ICBC_SIMD, icbc.h:59-117): the
+ * cluster-fit loops (icbc.h:2089-2344, :2362-2742) run over vectors of 4, 8
+ * or 16 combinations whose lanes keep their own minimum, fuse vmadd/vmsub on
+ * AVX2 and AVX-512 (icbc.h:734-752, :970-976) and round vround01 half to
+ * even from SSE4.1 on (icbc.h:518-524, :764-766, :988-990).  These entry
+ * points reproduce the output of such a build compiled without FP
+ * contraction (-ffp-contract=off), for callers whose stored assets came from
+ * one.  Profile ICBC_GPU_SIMD_SCALAR (and levels 0-1, which have no cluster
+ * fit) is the plain path.  Same arguments and results otherwise as
+ * icbc_gpu_compress_bc1_blocks / icbc_gpu_compress_bc1_image, which they
+ * replace for that build (icbc.h:48, :3846).  NEON (ICBC_SIMD=-1) is not
+ * offered: its vmlaq_f32 / vmlsq_f32 fuse or not with the compiler's
+ * contraction setting, so its output is not fixed by the source.
+ * ---------------------------------------------------------------------- */
+enum {
+    ICBC_GPU_SIMD_SCALAR = 0, /* ICBC_SIMD=0 (the plain path) */
+    ICBC_GPU_SIMD_SSE2 = 1,   /* 4 lanes, vround01 = int(x + 0.5f) */
+    ICBC_GPU_SIMD_SSE41 = 2,  /* 4 lanes, half to even */
+    ICBC_GPU_SIMD_AVX = 3,    /* 8 lanes, half to even */
+    ICBC_GPU_SIMD_AVX2 = 4,   /* 8 lanes, half to even, fused vmadd/vmsub */
+    ICBC_GPU_SIMD_AVX512 = 5  /* 16 lanes, half to even, fused vmadd/vmsub */
+};
+int icbc_gpu_compress_bc1_blocks_simd(int simd_profile, int level, const float *d_colors, const float *d_weights,
+                                      const float color_weights[3], int three_color_mode, int three_color_black,
+                                      int decoder, void *d_out, float *d_errors, int64_t n_blocks, void *stream);
+int icbc_gpu_compress_bc1_image_simd(int simd_profile, const icbc_gpu_image *image, void *stream);
+
 /* Batched form: many images of any size, level and decoder in one persistent
  * launch that drains a device work queue of (image, block range) tiles,
  * largest cost first.  A batch is planned once and can be launched many

@@ -70,6 +70,28 @@ static const float k_mid6[64] = {
     0.772549f, 0.788235f, 0.803922f, 0.819608f, 0.835294f, 0.850980f, 0.866667f, 0.882353f,
     0.898039f, 0.913725f, 0.929412f, 0.945098f, 0.960784f, 0.976471f, 0.992157f, FLT_MAX};
 
+/* SIMD profiles of the reference (ICBC_SIMD, icbc.h:59-66): the vector
+ * width of the cluster-fit loops, whether vmadd/vmsub are fused (AVX2 and
+ * AVX-512: icbc.h:734-752, :970-980) and whether vround01 rounds half to even
+ * (SSE4.1 and later: icbc.h:518-524, :764-766, :988-990) instead of
+ * int(x + 0.5f) (scalar, SSE2: icbc.h:417, :522).  Index 0 is the scalar
+ * profile; 1..5 are ICBC_SSE2, ICBC_SSE41, ICBC_AVX1, ICBC_AVX2, ICBC_AVX512. */
+typedef struct { int vec, fma, rne; } prof_t;
+static const prof_t k_prof[6] = {{1, 0, 0}, {4, 0, 0}, {4, 0, 1}, {8, 0, 1}, {8, 1, 1}, {16, 1, 1}};
+
+static inline float p_madd(const prof_t *p, float a, float b, float c) { return p->fma ? fmaf(a, b, c) : a * b + c; }
+static inline float p_msub(const prof_t *p, float a, float b, float c) { return p->fma ? fmaf(a, b, -c) : a * b - c; }
+/* vm2sub(a, b, c, d) = vmsub(a, b, c * d) (icbc.h:415, :754-756, :978-980). */
+static inline float p_m2sub(const prof_t *p, float a, float b, float c, float d) { return p_msub(p, a, b, c * d); }
+static inline float p_round01(const prof_t *p, float a) { return p->rne ? nearbyintf(a) : (float)(int)(a + 0.5f); }
+static inline v3 p_round_ept(const prof_t *p, v3 v) {
+    v3 r;
+    r.x = p_round01(p, vsaturate(v.x) * 31.0f) * (1.0f / 31.0f);
+    r.y = p_round01(p, vsaturate(v.y) * 63.0f) * (1.0f / 63.0f);
+    r.z = p_round01(p, vsaturate(v.z) * 31.0f) * (1.0f / 31.0f);
+    return r;
+}
+
 /* vround5 / vround6 / vround_ept without ICBC_PERFECT_ROUND (icbc.h:1588-1622). */
 static inline float vround5(float x) { return vround01(x * 31.0f) * (1.0f / 31.0f); }
 static inline float vround6(float x) { return vround01(x * 63.0f) * (1.0f / 63.0f); }
@@ -421,18 +443,37 @@ static int compute_sat(const v3 *colors, const float *weights, int count, sat_t 
 
 /* ---------------------------------------------------------- cluster fit */
 
-/* cluster_fit_three, scalar path: every 2-boundary split of the sorted
+/* The cross-lane argmin of the SIMD loops (reduce_min_index, icbc.h:574-586,
+ * :812-831, :1031-1039): the smallest per-lane best error, ties to the lowest
+ * lane (-0 and +0 compare equal).  Lane l kept the first strict minimum of the
+ * combinations l, l + vec, l + 2 vec, ... */
+static int lane_argmin(const float *best, int vec) {
+    float m = best[0];
+    for (int l = 1; l < vec; l++) m = best[l] < m ? best[l] : m;
+    for (int l = 0; l < vec; l++)
+        if (best[l] <= m) return l;
+    return 0;
+}
+
+/* cluster_fit_three (icbc.h:2075-2345): every 2-boundary split of the sorted
  * colours, least-squares endpoints with weights 1/2, snapped to 565, the
- * first strict minimum of the metric-weighted error kept (icbc.h:2075-2345). */
-static void cluster_fit_three(const sat_t *sat, int count, v3 metric_sqr, v3 *start, v3 *end, oracle_stats *st) {
+ * minimum metric-weighted error kept.  The loop runs over whole vectors of
+ * the profile's width: the combinations past the count's total come from
+ * the table for larger counts (or its zero padding) and read the SAT's
+ * FLT_MAX fill, as the reference's SIMD builds do. */
+static void cluster_fit_three(const sat_t *sat, int count, v3 metric_sqr, const prof_t *pf, v3 *start, v3 *end,
+                              oracle_stats *st) {
     const float r_sum = sat->r[count - 1], g_sum = sat->g[count - 1], b_sum = sat->b[count - 1], w_sum = sat->w[count - 1];
-    float best = FLT_MAX;
-    v3 bs = {0, 0, 0}, be = {0, 0, 0};
+    float best[16];
+    v3 bs[16], be[16];
+    for (int l = 0; l < 16; l++) { best[l] = FLT_MAX; bs[l] = be[l] = v3_make(0, 0, 0); }
     const int total = g_three_total[count - 1];
-    for (int i = 0; i < total; i++) {
+    const int padded = (total + pf->vec - 1) / pf->vec * pf->vec;
+    for (int i = 0; i < padded; i++) {
+        const int l = i % pf->vec;
         v3 x0 = {0, 0, 0}, x1 = {0, 0, 0};
         float w0 = 0, w1 = 0;
-        int c0 = g_three[i][0] - 1, c1 = g_three[i][1] - 1;
+        int c0 = (i < 152 ? g_three[i][0] : 0) - 1, c1 = (i < 152 ? g_three[i][1] : 0) - 1;
         if (c0 >= 0) { x0 = v3_make(sat->r[c0], sat->g[c0], sat->b[c0]); w0 = sat->w[c0]; }
         if (c1 >= 0) { x1 = v3_make(sat->r[c1], sat->g[c1], sat->b[c1]); w1 = sat->w[c1]; }
         float w2 = w_sum - w1;
@@ -441,46 +482,52 @@ static void cluster_fit_three(const sat_t *sat, int count, v3 metric_sqr, v3 *st
         float alphabeta_sum = w1 * 0.25f;
         float alpha2_sum = w0 + alphabeta_sum;
         float beta2_sum = w2 + alphabeta_sum;
-        float factor = 1.0f / (alpha2_sum * beta2_sum - alphabeta_sum * alphabeta_sum);
+        float factor = 1.0f / p_m2sub(pf, alpha2_sum, beta2_sum, alphabeta_sum, alphabeta_sum);
         v3 alphax_sum = v3_add(x0, v3_scale(x1, 0.5f));
         v3 betax_sum = v3_sub(v3_make(r_sum, g_sum, b_sum), alphax_sum);
         v3 a, b;
-        a.x = (alphax_sum.x * beta2_sum - betax_sum.x * alphabeta_sum) * factor;
-        a.y = (alphax_sum.y * beta2_sum - betax_sum.y * alphabeta_sum) * factor;
-        a.z = (alphax_sum.z * beta2_sum - betax_sum.z * alphabeta_sum) * factor;
-        b.x = (betax_sum.x * alpha2_sum - alphax_sum.x * alphabeta_sum) * factor;
-        b.y = (betax_sum.y * alpha2_sum - alphax_sum.y * alphabeta_sum) * factor;
-        b.z = (betax_sum.z * alpha2_sum - alphax_sum.z * alphabeta_sum) * factor;
-        a = vround_ept(a);
-        b = vround_ept(b);
-        /* e2 = vm2sub(a, vmsub(b, ab, ax), b, bx) * 2 ; e1 = a*a*alpha2 + (b*b*beta2 + e2) */
+        a.x = p_m2sub(pf, alphax_sum.x, beta2_sum, betax_sum.x, alphabeta_sum) * factor;
+        a.y = p_m2sub(pf, alphax_sum.y, beta2_sum, betax_sum.y, alphabeta_sum) * factor;
+        a.z = p_m2sub(pf, alphax_sum.z, beta2_sum, betax_sum.z, alphabeta_sum) * factor;
+        b.x = p_m2sub(pf, betax_sum.x, alpha2_sum, alphax_sum.x, alphabeta_sum) * factor;
+        b.y = p_m2sub(pf, betax_sum.y, alpha2_sum, alphax_sum.y, alphabeta_sum) * factor;
+        b.z = p_m2sub(pf, betax_sum.z, alpha2_sum, alphax_sum.z, alphabeta_sum) * factor;
+        a = p_round_ept(pf, a);
+        b = p_round_ept(pf, b);
+        /* e2 = vm2sub(a, vmsub(b, ab, ax), b, bx) * 2 ; e1 = vmadd(a*a, alpha2, vmadd(b*b, beta2, e2)) */
         v3 e2, e1;
-        e2.x = (a.x * (b.x * alphabeta_sum - alphax_sum.x) - b.x * betax_sum.x) * 2.0f;
-        e2.y = (a.y * (b.y * alphabeta_sum - alphax_sum.y) - b.y * betax_sum.y) * 2.0f;
-        e2.z = (a.z * (b.z * alphabeta_sum - alphax_sum.z) - b.z * betax_sum.z) * 2.0f;
-        e1.x = (a.x * a.x) * alpha2_sum + ((b.x * b.x) * beta2_sum + e2.x);
-        e1.y = (a.y * a.y) * alpha2_sum + ((b.y * b.y) * beta2_sum + e2.y);
-        e1.z = (a.z * a.z) * alpha2_sum + ((b.z * b.z) * beta2_sum + e2.z);
+        e2.x = p_m2sub(pf, a.x, p_msub(pf, b.x, alphabeta_sum, alphax_sum.x), b.x, betax_sum.x) * 2.0f;
+        e2.y = p_m2sub(pf, a.y, p_msub(pf, b.y, alphabeta_sum, alphax_sum.y), b.y, betax_sum.y) * 2.0f;
+        e2.z = p_m2sub(pf, a.z, p_msub(pf, b.z, alphabeta_sum, alphax_sum.z), b.z, betax_sum.z) * 2.0f;
+        e1.x = p_madd(pf, a.x * a.x, alpha2_sum, p_madd(pf, b.x * b.x, beta2_sum, e2.x));
+        e1.y = p_madd(pf, a.y * a.y, alpha2_sum, p_madd(pf, b.y * b.y, beta2_sum, e2.y));
+        e1.z = p_madd(pf, a.z * a.z, alpha2_sum, p_madd(pf, b.z * b.z, beta2_sum, e2.z));
         float error = v3_dot(e1, metric_sqr);
-        if (error < best) { best = error; bs = a; be = b; }
+        if (error < best[l]) { best[l] = error; bs[l] = a; be[l] = b; }
     }
     if (st) st->cf3_combos += total;
-    *start = bs;
-    *end = be;
+    const int w = lane_argmin(best, pf->vec);
+    *start = bs[w];
+    *end = be[w];
 }
 
-/* cluster_fit_four, scalar path (icbc.h:2348-2743) with the decoder's
- * interpolation weights w1_3, w2_3, w1_9, w4_9, w2_9. */
-static void cluster_fit_four(const sat_t *sat, int count, v3 metric_sqr, const dec_tables *dt, v3 *start, v3 *end, oracle_stats *st) {
+/* cluster_fit_four (icbc.h:2348-2743) with the decoder's interpolation
+ * weights w1_3, w2_3, w1_9, w4_9, w2_9; vector loop as cluster_fit_three. */
+static void cluster_fit_four(const sat_t *sat, int count, v3 metric_sqr, const dec_tables *dt, const prof_t *pf,
+                             v3 *start, v3 *end, oracle_stats *st) {
     const float r_sum = sat->r[count - 1], g_sum = sat->g[count - 1], b_sum = sat->b[count - 1], w_sum = sat->w[count - 1];
     const float w1_3 = dt->w1_3, w2_3 = dt->w2_3, w1_9 = dt->w1_9, w4_9 = dt->w4_9, w2_9 = dt->w2_9;
-    float best = FLT_MAX;
-    v3 bs = {0, 0, 0}, be = {0, 0, 0};
+    float best[16];
+    v3 bs[16], be[16];
+    for (int l = 0; l < 16; l++) { best[l] = FLT_MAX; bs[l] = be[l] = v3_make(0, 0, 0); }
     const int total = g_four_total[count - 1];
-    for (int i = 0; i < total; i++) {
+    const int padded = (total + pf->vec - 1) / pf->vec * pf->vec;
+    for (int i = 0; i < padded; i++) {
+        const int l = i % pf->vec;
         v3 x0 = {0, 0, 0}, x1 = {0, 0, 0}, x2 = {0, 0, 0};
         float w0 = 0, w1 = 0, w2 = 0;
-        int c0 = g_four[i][0] - 1, c1 = g_four[i][1] - 1, c2 = g_four[i][2] - 1;
+        int c0 = (i < 968 ? g_four[i][0] : 0) - 1, c1 = (i < 968 ? g_four[i][1] : 0) - 1;
+        int c2 = (i < 968 ? g_four[i][2] : 0) - 1;
         if (c0 >= 0) { x0 = v3_make(sat->r[c0], sat->g[c0], sat->b[c0]); w0 = sat->w[c0]; }
         if (c1 >= 0) { x1 = v3_make(sat->r[c1], sat->g[c1], sat->b[c1]); w1 = sat->w[c1]; }
         if (c2 >= 0) { x2 = v3_make(sat->r[c2], sat->g[c2], sat->b[c2]); w2 = sat->w[c2]; }
@@ -489,37 +536,38 @@ static void cluster_fit_four(const sat_t *sat, int count, v3 metric_sqr, const d
         x1 = v3_sub(x1, x0);
         w2 = w2 - w1;
         w1 = w1 - w0;
-        float alpha2_sum = w2 * w1_9 + (w1 * w4_9 + w0);
-        float beta2_sum = w1 * w1_9 + (w2 * w4_9 + w3);
+        float alpha2_sum = p_madd(pf, w2, w1_9, p_madd(pf, w1, w4_9, w0));
+        float beta2_sum = p_madd(pf, w1, w1_9, p_madd(pf, w2, w4_9, w3));
         float alphabeta_sum = (w1 + w2) * w2_9;
-        float factor = 1.0f / (alpha2_sum * beta2_sum - alphabeta_sum * alphabeta_sum);
+        float factor = 1.0f / p_m2sub(pf, alpha2_sum, beta2_sum, alphabeta_sum, alphabeta_sum);
         v3 alphax_sum;
-        alphax_sum.x = x2.x * w1_3 + (x1.x * w2_3 + x0.x);
-        alphax_sum.y = x2.y * w1_3 + (x1.y * w2_3 + x0.y);
-        alphax_sum.z = x2.z * w1_3 + (x1.z * w2_3 + x0.z);
+        alphax_sum.x = p_madd(pf, x2.x, w1_3, p_madd(pf, x1.x, w2_3, x0.x));
+        alphax_sum.y = p_madd(pf, x2.y, w1_3, p_madd(pf, x1.y, w2_3, x0.y));
+        alphax_sum.z = p_madd(pf, x2.z, w1_3, p_madd(pf, x1.z, w2_3, x0.z));
         v3 betax_sum = v3_sub(v3_make(r_sum, g_sum, b_sum), alphax_sum);
         v3 a, b;
-        a.x = (alphax_sum.x * beta2_sum - betax_sum.x * alphabeta_sum) * factor;
-        a.y = (alphax_sum.y * beta2_sum - betax_sum.y * alphabeta_sum) * factor;
-        a.z = (alphax_sum.z * beta2_sum - betax_sum.z * alphabeta_sum) * factor;
-        b.x = (betax_sum.x * alpha2_sum - alphax_sum.x * alphabeta_sum) * factor;
-        b.y = (betax_sum.y * alpha2_sum - alphax_sum.y * alphabeta_sum) * factor;
-        b.z = (betax_sum.z * alpha2_sum - alphax_sum.z * alphabeta_sum) * factor;
-        a = vround_ept(a);
-        b = vround_ept(b);
+        a.x = p_m2sub(pf, alphax_sum.x, beta2_sum, betax_sum.x, alphabeta_sum) * factor;
+        a.y = p_m2sub(pf, alphax_sum.y, beta2_sum, betax_sum.y, alphabeta_sum) * factor;
+        a.z = p_m2sub(pf, alphax_sum.z, beta2_sum, betax_sum.z, alphabeta_sum) * factor;
+        b.x = p_m2sub(pf, betax_sum.x, alpha2_sum, alphax_sum.x, alphabeta_sum) * factor;
+        b.y = p_m2sub(pf, betax_sum.y, alpha2_sum, alphax_sum.y, alphabeta_sum) * factor;
+        b.z = p_m2sub(pf, betax_sum.z, alpha2_sum, alphax_sum.z, alphabeta_sum) * factor;
+        a = p_round_ept(pf, a);
+        b = p_round_ept(pf, b);
         v3 e2, e1;
-        e2.x = (a.x * (b.x * alphabeta_sum - alphax_sum.x) - b.x * betax_sum.x) * 2.0f;
-        e2.y = (a.y * (b.y * alphabeta_sum - alphax_sum.y) - b.y * betax_sum.y) * 2.0f;
-        e2.z = (a.z * (b.z * alphabeta_sum - alphax_sum.z) - b.z * betax_sum.z) * 2.0f;
-        e1.x = (a.x * a.x) * alpha2_sum + ((b.x * b.x) * beta2_sum + e2.x);
-        e1.y = (a.y * a.y) * alpha2_sum + ((b.y * b.y) * beta2_sum + e2.y);
-        e1.z = (a.z * a.z) * alpha2_sum + ((b.z * b.z) * beta2_sum + e2.z);
+        e2.x = p_m2sub(pf, a.x, p_msub(pf, b.x, alphabeta_sum, alphax_sum.x), b.x, betax_sum.x) * 2.0f;
+        e2.y = p_m2sub(pf, a.y, p_msub(pf, b.y, alphabeta_sum, alphax_sum.y), b.y, betax_sum.y) * 2.0f;
+        e2.z = p_m2sub(pf, a.z, p_msub(pf, b.z, alphabeta_sum, alphax_sum.z), b.z, betax_sum.z) * 2.0f;
+        e1.x = p_madd(pf, a.x * a.x, alpha2_sum, p_madd(pf, b.x * b.x, beta2_sum, e2.x));
+        e1.y = p_madd(pf, a.y * a.y, alpha2_sum, p_madd(pf, b.y * b.y, beta2_sum, e2.y));
+        e1.z = p_madd(pf, a.z * a.z, alpha2_sum, p_madd(pf, b.z * b.z, beta2_sum, e2.z));
         float error = v3_dot(e1, metric_sqr);
-        if (error < best) { best = error; bs = a; be = b; }
+        if (error < best[l]) { best[l] = error; bs[l] = a; be[l] = b; }
     }
     if (st) st->cf4_combos += total;
-    *start = bs;
-    *end = be;
+    const int w = lane_argmin(best, pf->vec);
+    *start = bs[w];
+    *end = be[w];
 }
 
 /* ------------------------------------------------------ error evaluation */
@@ -715,12 +763,12 @@ static void single_color(c32 c, const dec_tables *dt, blk *out) {
 /* compress_dxt1_cluster_fit (icbc.h:3537-3571). */
 static float cluster_fit(const float *in, const float *in_w, const v3 *colors, const float *weights, int count,
                          v3 cw, int three_color_mode, int try_black, int allow_black, int decoder,
-                         const dec_tables *dt, blk *out, oracle_stats *st) {
+                         const dec_tables *dt, const prof_t *pf, blk *out, oracle_stats *st) {
     v3 metric_sqr = v3_mul(cw, cw);
     sat_t sat;
     int sat_count = compute_sat(colors, weights, count, &sat, st);
     v3 start, end;
-    cluster_fit_four(&sat, sat_count, metric_sqr, dt, &start, &end, st);
+    cluster_fit_four(&sat, sat_count, metric_sqr, dt, pf, &start, &end, st);
     float best = output_block4(in, in_w, cw, start, end, decoder, out, st);
     if (three_color_mode) {
         if (try_black) {
@@ -730,7 +778,7 @@ static float cluster_fit(const float *in, const float *in_w, const v3 *colors, c
             if (!tcount) return best;
             sat_count = compute_sat(tc, tw, tcount, &sat, st);
         }
-        cluster_fit_three(&sat, sat_count, metric_sqr, &start, &end, st);
+        cluster_fit_three(&sat, sat_count, metric_sqr, pf, &start, &end, st);
         blk b3;
         float e3 = output_block3(in, in_w, cw, allow_black, start, end, decoder, &b3, st);
         if (e3 < best) { best = e3; *out = b3; }
@@ -829,6 +877,8 @@ static void load_block(const void *in, blk *b) {
 float oracle_compress_bc1(int decoder, int level, const float *in, const float *in_w, const float cwa[3],
                           int three_color_mode, int three_color_black, void *outp, oracle_stats *st) {
     oracle_init();
+    int profile = (decoder >> ORACLE_PROFILE_SHIFT) & 7;
+    const prof_t *pf = &k_prof[profile < 6 ? profile : 0];
     decoder &= 3;
     const dec_tables *dt = &g_dec[decoder];
     options opt = setup_options(level, three_color_mode, three_color_black);
@@ -883,7 +933,7 @@ float oracle_compress_bc1(int decoder, int level, const float *in, const float *
         int use_three = opt.cluster_fit_3 || (use_black && opt.cluster_fit_3_black_only);
         blk cb;
         float ce = cluster_fit(in, in_w, colors, weights, count, cw, use_three, use_black, three_color_black,
-                               decoder, dt, &cb, st);
+                               decoder, dt, pf, &cb, st);
         if (ce < error) { out = cb; error = ce; }
     }
     if (opt.endpoint_refinement)

@@ -7,7 +7,12 @@ package ``icbc_gb300``.
 * ``liboracle.so`` is the C restatement in ``icbc_oracle.c`` (built here with
   gcc, on any host).
 * ``_ref/libicbc_ref.so`` is the reference's own icbc.h in its scalar profile,
-  built by ``build_ref.sh`` only where the reference checkout exists.
+  built by ``build_ref.sh`` only where the reference checkout exists;
+  ``_ref/libicbc_ref_simd<N>.so`` are its x86 SIMD builds (N = ICBC_SIMD 1..5).
+
+SIMD profiles: every ``decoder`` below may be combined with ``profile``
+(0 scalar, 1 SSE2, 2 SSE4.1, 3 AVX, 4 AVX2, 5 AVX-512); the oracle then
+reproduces that build's cluster-fit loops.
 """
 from __future__ import annotations
 
@@ -24,7 +29,14 @@ REF_PATH = os.path.join(HERE, "_ref", "libicbc_ref.so")
 
 _lock = threading.Lock()
 _lib = None
-_ref = None
+_ref = {}
+
+PROFILE_SHIFT = 8
+PROFILES = {"scalar": 0, "sse2": 1, "sse41": 2, "avx": 3, "avx2": 4, "avx512": 5}
+
+
+def ref_path(profile: int = 0) -> str:
+    return REF_PATH if profile == 0 else os.path.join(HERE, "_ref", "libicbc_ref_simd%d.so" % profile)
 
 CFLAGS = ["-O2", "-std=c99", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread"]
 
@@ -102,19 +114,20 @@ def lib():
     return _lib
 
 
-def ref():
-    """The compiled reference, or None where it cannot be built."""
-    global _ref
+def ref(profile: int = 0):
+    """The compiled reference (scalar build, or the x86 SIMD build `profile`),
+    or None where it cannot be built."""
     with _lock:
-        if _ref is None:
-            if not os.path.exists(REF_PATH):
+        if profile not in _ref:
+            path = ref_path(profile)
+            if not os.path.exists(path):
                 try:
                     build_ref()
                 except Exception:
                     return None
-            if not os.path.exists(REF_PATH):
+            if not os.path.exists(path):
                 return None
-            R = ctypes.CDLL(REF_PATH)
+            R = ctypes.CDLL(path)
             R.ref_init.restype = None
             R.ref_init.argtypes = [ctypes.c_int]
             R.ref_compress_blocks.restype = None
@@ -125,8 +138,19 @@ def ref():
             R.ref_decode_bc1.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
             R.ref_evaluate_bc1_error.restype = ctypes.c_float
             R.ref_evaluate_bc1_error.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
-            _ref = R
-    return _ref
+            _ref[profile] = R
+    return _ref[profile]
+
+
+def _aligned_f32(a, align: int = 64):
+    """A float32 copy of `a` whose data starts on an `align`-byte boundary
+    (the SIMD builds load input colours with aligned vector loads)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    buf = np.empty(a.size + align // 4, np.float32)
+    off = (-buf.ctypes.data % align) // 4
+    out = buf[off:off + a.size].reshape(a.shape)
+    out[...] = a
+    return out
 
 
 def _f32(a):
@@ -139,7 +163,7 @@ def _cw(color_weights):
 
 
 def compress_blocks(colors, weights, level, decoder=0, color_weights=(1, 1, 1), three_color_mode=True,
-                    three_color_black=True, nthreads=1, out=None, with_stats=False):
+                    three_color_black=True, nthreads=1, out=None, with_stats=False, profile=0):
     """Oracle encode of n blocks.  colors: (n,16,4) float32; weights: (n,16) or None.
     Returns (blocks uint8 (n,8), errors float32 (n,)[, stats dict])."""
     L = lib()
@@ -150,14 +174,15 @@ def compress_blocks(colors, weights, level, decoder=0, color_weights=(1, 1, 1), 
     err = np.zeros(n, np.float32)
     cw, cwp = _cw(color_weights)
     st = Stats()
-    L.oracle_compress_blocks(int(decoder), int(level), colors.ctypes.data, None if w is None else w.ctypes.data,
+    L.oracle_compress_blocks(int(decoder) | (int(profile) << PROFILE_SHIFT), int(level), colors.ctypes.data,
+                             None if w is None else w.ctypes.data,
                              cwp, int(bool(three_color_mode)), int(bool(three_color_black)), out.ctypes.data,
                              err.ctypes.data, n, int(nthreads), ctypes.byref(st))
     return (out, err, st.as_dict()) if with_stats else (out, err)
 
 
 def encode_image(rgba, level, decoder=0, color_weights=(1, 1, 1), weight_mode=0, weight_plane=None,
-                 three_color_mode=True, three_color_black=True, nthreads=1, with_stats=False):
+                 three_color_mode=True, three_color_black=True, nthreads=1, with_stats=False, profile=0):
     """Oracle encode of an RGBA8 image (h, w, 4) uint8 -> (blocks (nb,8), errors (nb,))."""
     L = lib()
     rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
@@ -169,7 +194,8 @@ def encode_image(rgba, level, decoder=0, color_weights=(1, 1, 1), weight_mode=0,
     plane = None if weight_plane is None else _f32(weight_plane).reshape(h, w)
     st = Stats()
     L.oracle_encode_image(rgba.ctypes.data, w, h, w * 4, int(weight_mode),
-                          None if plane is None else plane.ctypes.data, int(decoder), int(level), cwp,
+                          None if plane is None else plane.ctypes.data, int(decoder) | (int(profile) << PROFILE_SHIFT),
+                          int(level), cwp,
                           int(bool(three_color_mode)), int(bool(three_color_black)), out.ctypes.data,
                           err.ctypes.data, int(nthreads), ctypes.byref(st))
     return (out, err, st.as_dict()) if with_stats else (out, err)
@@ -243,12 +269,12 @@ def cluster_tables():
 
 
 def ref_compress_blocks(colors, weights, level, decoder=0, color_weights=(1, 1, 1), three_color_mode=True,
-                        three_color_black=True, out=None):
+                        three_color_black=True, out=None, profile=0):
     """The compiled reference (single thread) on the same inputs.  None if unavailable."""
-    R = ref()
+    R = ref(profile)
     if R is None:
         return None
-    colors = _f32(colors).reshape(-1, 64)
+    colors = _aligned_f32(_f32(colors).reshape(-1, 64))
     n = colors.shape[0]
     w = np.ones((n, 16), np.float32) if weights is None else _f32(weights).reshape(n, 16)
     out = np.zeros((n, 8), np.uint8) if out is None else np.ascontiguousarray(out, dtype=np.uint8).copy()

@@ -13,8 +13,14 @@ stores inputs and outputs:
                three-colour flags on; plus the SHA-256 of the generated image
   decode.npz   decode_bc1 and evaluate_bc1_error of the reference for every
                decoder on encoded blocks, including 3-colour blocks
+  simd.npz     the reference's x86 SIMD builds (ICBC_SIMD 1..5, compiled
+               without FP contraction by the same script) on two sets of 128
+               image blocks -- the blocks of two 512x512 images where some
+               SIMD build differs from the scalar one, topped up with the
+               first others -- at levels 2, 4, 8, 9 x decoder x
+               (three_color_mode, three_color_black) in {(1, 1), (0, 0)}
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [simd]   (simd: only simd.npz)
 """
 from __future__ import annotations
 
@@ -65,9 +71,57 @@ def golden_blocks(n_mixed: int = 224) -> tuple[np.ndarray, np.ndarray]:
     return (np.concatenate([cols, np.stack(extra_c)]), np.concatenate([w, np.stack(extra_w)]))
 
 
+SIMD_LEVELS = (2, 4, 8, 9)
+SIMD_FLAGS = ((1, 1), (0, 0))
+
+
+def simd_sets(per_set: int = 128):
+    """Two block sets (colors, weights, cw) where the SIMD builds matter."""
+    sets = []
+    for img, wm, cw in ((synth.gradient_noise_rects(512, 512, 1), 0, (1.0, 1.0, 1.0)),
+                        (synth.quality_sweep_image(512, 512, seed=4), 1, (0.299, 0.587, 0.114))):
+        cols, w, _ = O.image_blocks(img, weight_mode=wm)
+        differ = np.zeros(cols.shape[0], bool)
+        for lvl in (4, 8):
+            base, _ = O.compress_blocks(cols, w, lvl, 0, cw, True, True, nthreads=os.cpu_count() or 1)
+            for prof in range(1, 6):
+                b, _ = O.compress_blocks(cols, w, lvl, 0, cw, True, True, nthreads=os.cpu_count() or 1,
+                                         profile=prof)
+                differ |= (b != base).any(1)
+        pick = list(np.flatnonzero(differ)[:per_set])
+        pick += [i for i in range(cols.shape[0]) if not differ[i]][:per_set - len(pick)]
+        pick = np.array(sorted(pick))
+        wt = np.ones((len(pick), 16), np.float32) if w is None else w[pick]
+        sets.append((np.ascontiguousarray(cols[pick]), np.ascontiguousarray(wt), cw))
+    return sets
+
+
+def golden_simd():
+    out = {}
+    for si, (cols, wt, cw) in enumerate(simd_sets()):
+        out["set%d_colors" % si] = cols
+        out["set%d_weights" % si] = wt
+        out["set%d_cw" % si] = np.array(cw, np.float32)
+        for prof in range(1, 6):
+            if O.ref(prof) is None:
+                raise SystemExit("the x86 SIMD builds of the reference are needed for simd.npz")
+            for lvl in SIMD_LEVELS:
+                for dec in range(4):
+                    for tc, tcb in SIMD_FLAGS:
+                        b, e = O.ref_compress_blocks(cols, wt, lvl, dec, cw, tc, tcb, profile=prof)
+                        key = "set%d_P%d_L%d_D%d_tc%d_tcb%d" % (si, prof, lvl, dec, tc, tcb)
+                        out[key + "_blocks"] = b
+                        out[key + "_errors"] = e
+    np.savez_compressed(os.path.join(HERE, "simd.npz"), **out)
+    print("simd.npz", os.path.getsize(os.path.join(HERE, "simd.npz")))
+
+
 def main():
     if O.ref() is None:
         raise SystemExit("the reference checkout is needed to generate golden vectors")
+    if sys.argv[1:] == ["simd"]:
+        golden_simd()
+        return
     colors, wr = golden_blocks()
     n = colors.shape[0]
     wu = np.ones((n, 16), np.float32)
@@ -105,6 +159,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "decode.npz"), **dec_out)
     for f in ("blocks.npz", "image512.npz", "decode.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
+    golden_simd()
 
 
 if __name__ == "__main__":

@@ -208,6 +208,32 @@ def test_batch_level9_refinement_pass(gpu_lib):
         assert same_bits(err.cpu().numpy(), oe), c
 
 
+def test_batch_with_own_launch_images(gpu_lib):
+    """Images of 2^20 blocks or more run as their level's own kernels inside
+    the batch graph (level 9 with the batch's refinement slots); the rest
+    share the batch kernel.  Both kinds equal the plain launches, twice."""
+    import torch
+    ig = gpu_lib
+    specs = [(4096, 4096, 9, 0), (4100, 4096, 2, 1), (64, 64, 9, 2), (100, 52, 5, 3), (33, 17, 9, 0)]
+    descs, outs, plains, devs = [], [], [], []  # the descriptors hold raw pointers: keep the images alive
+    for i, (w, h, level, dec) in enumerate(specs):
+        dev = synth.hard_mixture_torch(w, h, 50 + i, torch.device("cuda")) if w >= 4096 else \
+            _to_dev(synth.quality_sweep_image(w, h, seed=60 + i))
+        devs.append(dev)
+        nb = ig.blocks_of(w, h)
+        out = torch.zeros((nb, 8), dtype=torch.uint8, device="cuda")
+        descs.append(ig.image_desc(dev, level, out, None, dec, (1, 1, 1), ig.WEIGHTS_ALPHA))
+        outs.append(out)
+        plains.append(ig.compress_image(dev, level, dec, (1, 1, 1), ig.WEIGHTS_ALPHA))
+    batch = ig.Batch(descs)
+    for _ in range(2):
+        batch.launch()
+        torch.cuda.synchronize()
+        for s_, out, p in zip(specs, outs, plains):
+            assert torch.equal(out, p), s_
+    batch.close()
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib

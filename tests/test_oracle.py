@@ -93,3 +93,43 @@ def test_oracle_prior_output_semantics():
         b, eb = O.ref_compress_blocks(cols, w, level, 0, (1, 1, 1), True, True, out=prior)
         assert np.array_equal(a, b)
         assert np.array_equal(ea.view(np.uint32), eb.view(np.uint32))
+
+
+SIMD_LEVELS = (2, 4, 8, 9)
+SIMD_FLAGS = ((1, 1), (0, 0))
+
+
+@pytest.mark.parametrize("profile", range(1, 6))
+def test_oracle_simd_profiles_match_golden(profile):
+    """The oracle's SIMD profiles against the golden vectors the reference's
+    SSE2 / SSE4.1 / AVX / AVX2 / AVX-512 builds produced."""
+    g = np.load(os.path.join(GOLDEN, "simd.npz"))
+    for si in range(2):
+        cols, wt, cw = g["set%d_colors" % si], g["set%d_weights" % si], tuple(g["set%d_cw" % si])
+        for lvl in SIMD_LEVELS:
+            for dec in range(4):
+                for tc, tcb in SIMD_FLAGS:
+                    key = "set%d_P%d_L%d_D%d_tc%d_tcb%d" % (si, profile, lvl, dec, tc, tcb)
+                    b, e = O.compress_blocks(cols, wt, lvl, dec, cw, tc, tcb, profile=profile)
+                    assert np.array_equal(b, g[key + "_blocks"]), key
+                    assert np.array_equal(e.view(np.uint32), g[key + "_errors"].view(np.uint32)), key
+
+
+@pytest.mark.parametrize("profile", range(1, 6))
+def test_oracle_simd_profiles_match_compiled_builds(profile):
+    """The same against the SIMD builds themselves on other blocks (x86 hosts
+    with the reference checkout only)."""
+    if O.ref(profile) is None:
+        pytest.skip("the reference's SIMD builds are not available here")
+    cols, w = synth.mixed_blocks(400, seed=21)
+    img = synth.quality_sweep_image(128, 64, seed=9)
+    ci, wi, _ = O.image_blocks(img, weight_mode=1)
+    for c, wt in ((cols, w), (ci, wi)):
+        for lvl in SIMD_LEVELS:
+            for dec in range(4):
+                for tc, tcb in SIMD_FLAGS:
+                    cw = (0.299, 0.587, 0.114) if dec % 2 else (1.0, 1.0, 1.0)
+                    rb, re = O.ref_compress_blocks(c, wt, lvl, dec, cw, tc, tcb, profile=profile)
+                    ob, oe = O.compress_blocks(c, wt, lvl, dec, cw, tc, tcb, nthreads=4, profile=profile)
+                    assert np.array_equal(rb, ob), (lvl, dec, tc, tcb)
+                    assert np.array_equal(re.view(np.uint32), oe.view(np.uint32)), (lvl, dec, tc, tcb)
