@@ -130,6 +130,12 @@ def load(build_if_missing: bool = True):
             "icbc_gpu_server_get_stats": (i32, [vp, ctypes.POINTER(ServerStats)]),
             "icbc_gpu_server_destroy": (i32, [vp]),
             "icbc_gpu_write_dds": (i32, [ctypes.c_char_p, i32, i32, vp]),
+            "icbc_gpu_write_dds_mips": (i32, [ctypes.c_char_p, i32, i32, i32, vp]),
+            "icbc_gpu_expand_rgba8": (i32, [vp, i32, i32, i32, i64, vp, i64, vp]),
+            "icbc_gpu_mip_levels": (i32, [i32, i32]),
+            "icbc_gpu_mip_layout": (i32, [i32, i32, i32, vp, vp, vp]),
+            "icbc_gpu_build_mips": (i32, [vp, i32, i32, i64, i32, vp, vp]),
+            "icbc_gpu_compress_bc1_mips": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
             "icbc_gpu_set_launch_config": (i32, [i32, ctypes.POINTER(LaunchConfig)]),
             "icbc_gpu_get_launch_config": (i32, [i32, ctypes.POINTER(LaunchConfig)]),
             "icbc_gpu_write_ktx": (i32, [ctypes.c_char_p, i32, i32, vp]),
@@ -416,6 +422,73 @@ def write_dds(path: str, width: int, height: int, blocks) -> None:
     """DDS file (DXT1, one mip) of host (numpy) or device (torch) blocks."""
     b = blocks if hasattr(blocks, "data_ptr") else np.ascontiguousarray(blocks, np.uint8)
     _check(load().icbc_gpu_write_dds(os.fsencode(path), int(width), int(height), _blocks_ptr(b)), "write_dds")
+
+
+def write_dds_mips(path: str, width: int, height: int, levels: int, blocks) -> None:
+    """DDS file of a whole mip chain (blocks of every level, mip_layout order)."""
+    b = blocks if hasattr(blocks, "data_ptr") else np.ascontiguousarray(blocks, np.uint8)
+    _check(load().icbc_gpu_write_dds_mips(os.fsencode(path), int(width), int(height), int(levels), _blocks_ptr(b)),
+           "write_dds_mips")
+
+
+def expand_rgba8(pixels, stream=None):
+    """stbi_load(..., 4)-style expansion on the device: a CUDA uint8 tensor
+    (h, w, c) with c in 1..4 (or (h, w) grey) -> (h, w, 4) RGBA8."""
+    torch = _torch()
+    src = pixels if pixels.dim() == 3 else pixels.unsqueeze(-1)
+    h, w, c = (int(x) for x in src.shape)
+    src = src.contiguous()
+    out = torch.empty((h, w, 4), dtype=torch.uint8, device=src.device)
+    _check(load().icbc_gpu_expand_rgba8(src.data_ptr(), c, w, h, w * c, out.data_ptr(), 4 * w, _stream_ptr(stream)),
+           "expand_rgba8")
+    return out
+
+
+def mip_levels(width: int, height: int) -> int:
+    return int(load().icbc_gpu_mip_levels(int(width), int(height)))
+
+
+def mip_layout(width: int, height: int, levels: int | None = None):
+    """(widths, heights, block_offsets) of a chain (offsets has levels + 1 entries)."""
+    levels = mip_levels(width, height) if levels is None else int(levels)
+    ws, hs = (ctypes.c_int32 * levels)(), (ctypes.c_int32 * levels)()
+    off = (ctypes.c_int64 * (levels + 1))()
+    _check(load().icbc_gpu_mip_layout(int(width), int(height), levels, ws, hs, off), "mip_layout")
+    return list(ws), list(hs), list(off)
+
+
+def build_mips(rgba, levels: int | None = None, stream=None):
+    """Mip chain of a CUDA RGBA8 tensor (h, w, 4): a list of (h_k, w_k, 4)
+    tensors, level 0 being `rgba` itself."""
+    torch = _torch()
+    h, w = int(rgba.shape[0]), int(rgba.shape[1])
+    ws, hs, _ = mip_layout(w, h, levels)
+    total = sum(4 * ws[k] * hs[k] for k in range(1, len(ws)))
+    chain = torch.empty(max(total, 4), dtype=torch.uint8, device=rgba.device)
+    _check(load().icbc_gpu_build_mips(rgba.data_ptr(), w, h, int(rgba.stride(0)), len(ws), chain.data_ptr(),
+                                      _stream_ptr(stream)), "build_mips")
+    out, pos = [rgba], 0
+    for k in range(1, len(ws)):
+        n = 4 * ws[k] * hs[k]
+        out.append(chain[pos:pos + n].view(hs[k], ws[k], 4))
+        pos += n
+    return out
+
+
+def compress_mips(rgba, level: int, levels: int | None = None, decoder: int = DECODER_DEFAULT,
+                  color_weights=(1.0, 1.0, 1.0), weight_mode: int = WEIGHTS_UNIFORM, three_color_mode: bool = True,
+                  three_color_black: bool = True, with_errors: bool = False, stream=None):
+    """Builds the mip chain of a CUDA RGBA8 tensor (h, w, 4) and encodes every
+    level in one batch.  Returns (blocks (total, 8)[, errors], block_offsets)."""
+    torch = _torch()
+    h, w = int(rgba.shape[0]), int(rgba.shape[1])
+    ws, hs, off = mip_layout(w, h, levels)
+    out = torch.zeros((off[-1], 8), dtype=torch.uint8, device=rgba.device)
+    errors = torch.empty(off[-1], dtype=torch.float32, device=rgba.device) if with_errors else None
+    d = image_desc(rgba, level, out, errors, decoder, color_weights, weight_mode, None, three_color_mode,
+                   three_color_black)
+    _check(load().icbc_gpu_compress_bc1_mips(ctypes.byref(d), len(ws), _stream_ptr(stream)), "compress_bc1_mips")
+    return (out, errors, off) if with_errors else (out, off)
 
 
 def write_ktx(path: str, width: int, height: int, blocks) -> None:

@@ -42,7 +42,7 @@ def _units():
               for lv in range(9, -1, -1)]
     units += [(os.path.join(CSRC, n), [], n.replace(".cu", ".o"))
               for n in ("bc1_decode.cu", "icbc_gpu_api.cu", "icbc_gpu_serve.cu", "icbc_compat.cu", "bc1_refine.cu",
-                        "icbc_containers.cu")]
+                        "icbc_containers.cu", "bc1_ingest.cu")]
     return [u for u in units if os.path.exists(u[0])]
 
 

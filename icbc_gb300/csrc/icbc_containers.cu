@@ -37,24 +37,27 @@ void put32(std::vector<uint8_t> &v, uint32_t x) {
 }
 
 // The 128-byte DDS preamble: "DDS " and the 124-byte header (caps, pixel
-// format, width, height, linear size) with a DXT1 FourCC pixel format.
-std::vector<uint8_t> dds_header(int32_t w, int32_t h) {
+// format, width, height, linear size of the top level) with a DXT1 FourCC
+// pixel format; with more than one level also the mip count and the
+// complex / mipmap caps.
+std::vector<uint8_t> dds_header(int32_t w, int32_t h, int32_t levels = 1) {
     const uint32_t caps = 0x1, pixelformat = 0x1000, width = 0x4, height = 0x2, linearsize = 0x80000;
+    const uint32_t mipcount = levels > 1 ? 0x20000 : 0;
     std::vector<uint8_t> v;
     put32(v, fourcc("DDS "));
     put32(v, 124);
-    put32(v, caps | pixelformat | width | height | linearsize);
+    put32(v, caps | pixelformat | width | height | linearsize | mipcount);
     put32(v, (uint32_t)h);
     put32(v, (uint32_t)w);
     put32(v, (uint32_t)block_bytes(w, h));
     put32(v, 0);  // depth
-    put32(v, 1);  // mip levels
+    put32(v, (uint32_t)levels);  // mip levels
     for (int i = 0; i < 11; i++) put32(v, 0);
     put32(v, 32);     // pixel format size
     put32(v, 0x4);    // DDPF_FOURCC
     put32(v, fourcc("DXT1"));
     for (int i = 0; i < 5; i++) put32(v, 0);  // bit count, masks
-    put32(v, 0x1000);  // DDSCAPS_TEXTURE
+    put32(v, 0x1000 | (levels > 1 ? 0x400008u : 0u));  // DDSCAPS_TEXTURE (| MIPMAP | COMPLEX)
     for (int i = 0; i < 3; i++) put32(v, 0);
     put32(v, 0);
     return v;
@@ -80,6 +83,19 @@ int icbc_gpu_write_dds(const char *path, int32_t width, int32_t height, const vo
     const int st = host_blocks(blocks, bytes, copy, &data);
     if (st) return st;
     return write_file(path, dds_header(width, height), data, bytes);
+}
+
+int icbc_gpu_write_dds_mips(const char *path, int32_t width, int32_t height, int32_t levels, const void *blocks) {
+    if (!path || !blocks || width < 1 || height < 1 || levels < 1 || levels > icbc_gpu_mip_levels(width, height))
+        return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    size_t bytes = 0;
+    for (int32_t k = 0, w = width, h = height; k < levels; k++, w = w > 1 ? w >> 1 : 1, h = h > 1 ? h >> 1 : 1)
+        bytes += block_bytes(w, h);
+    std::vector<uint8_t> copy;
+    const uint8_t *data = nullptr;
+    const int st = host_blocks(blocks, bytes, copy, &data);
+    if (st) return st;
+    return write_file(path, dds_header(width, height, levels), data, bytes);
 }
 
 int icbc_gpu_write_ktx(const char *path, int32_t width, int32_t height, const void *blocks) {

@@ -278,12 +278,47 @@ int icbc_gpu_server_destroy(icbc_gpu_server *server);
  * ---------------------------------------------------------------------- */
 /* DDS with a DXT1 FourCC and one mip level (icbc_test.cpp:155-211). */
 int icbc_gpu_write_dds(const char *path, int32_t width, int32_t height, const void *blocks);
+/* DDS of a whole mip chain: `levels` levels (as icbc_gpu_mip_layout lays
+ * them out, level 0 first, blocks contiguous), mip count and mipmap caps set. */
+int icbc_gpu_write_dds_mips(const char *path, int32_t width, int32_t height, int32_t levels, const void *blocks);
 /* KTX 1.1, GL_COMPRESSED_RGB_S3TC_DXT1_EXT (icbc_test.cpp:233-279). */
 int icbc_gpu_write_ktx(const char *path, int32_t width, int32_t height, const void *blocks);
 /* Golden-file check (icbc_test.cpp:213-231): 1 when the DDS file's block
  * data equals `blocks`, 0 when it differs, a negative status on error
  * (-ICBC_GPU_ERR_NOT_FOUND: file missing or short). */
 int icbc_gpu_compare_dds(const char *path, int32_t width, int32_t height, const void *blocks);
+
+/* ------------------------------------------------------------------------
+ * Input side.  The reference's driver decodes files with
+ * stbi_load(..., 4) (icbc_test.cpp:345): 1..4-channel 8-bit pixels expanded
+ * to RGBA8.  icbc_gpu_expand_rgba8 does that expansion on the device (grey ->
+ * (g, g, g, 255), grey + alpha -> (g, g, g, a), RGB -> (r, g, b, 255), RGBA as
+ * is), so decoded pixels are uploaded as they are.  (The driver also drops
+ * partial edge blocks, icbc_test.cpp:353-358; pass width & ~3 and
+ * height & ~3 to get that.)
+ *
+ * Mip chains (no counterpart in the reference, which encodes one level; the
+ * role of its callers' texture pipelines): level k + 1 is
+ * max(1, w >> 1) x max(1, h >> 1), each channel (a + b + c + d + 2) >> 2 over
+ * the 2x2 source texels (2x, 2y) .. (2x + 1, 2y + 1), coordinates clamped to
+ * the source.  Levels down to 1 x 1: icbc_gpu_mip_levels(w, h).
+ * ---------------------------------------------------------------------- */
+int icbc_gpu_expand_rgba8(const uint8_t *d_src, int32_t channels, int32_t width, int32_t height, int64_t src_pitch,
+                          uint8_t *d_rgba, int64_t rgba_pitch, void *stream);
+int icbc_gpu_mip_levels(int32_t width, int32_t height);
+/* Sizes of levels 0..levels-1 and the first block of each in a chain's block
+ * array (levels + 1 offsets; the last is the total).  Any output may be NULL. */
+int icbc_gpu_mip_layout(int32_t width, int32_t height, int32_t levels, int32_t *widths, int32_t *heights,
+                        int64_t *block_offsets);
+/* Levels 1..levels-1 of d_rgba into d_chain, each tightly packed (pitch
+ * 4 * width), one after another.  Device pointers, 4-byte aligned. */
+int icbc_gpu_build_mips(const uint8_t *d_rgba, int32_t width, int32_t height, int64_t pitch, int32_t levels,
+                        uint8_t *d_chain, void *stream);
+/* Builds the chain of `image` and encodes its `levels` levels in one batch
+ * with the image's level, decoder, flags, colour weights and weight mode
+ * (uniform or alpha).  image->out (and image->errors, if set) receive every
+ * level's blocks at icbc_gpu_mip_layout's offsets.  Synchronous. */
+int icbc_gpu_compress_bc1_mips(const icbc_gpu_image *image, int32_t levels, void *stream);
 
 /* Launch shape of the plain kernels of one quality level, chosen by an
  * autotuner (icbc_gb300.autotune) or set by hand.  groups_per_warp: groups

@@ -307,3 +307,43 @@ def ref_evaluate_bc1_error(rgba_blocks, blocks, decoder=0):
     b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 8)
     return np.array([R.ref_evaluate_bc1_error(t[i].ctypes.data, b[i].ctypes.data, int(decoder))
                      for i in range(b.shape[0])], np.float32)
+
+
+def expand_rgba8(pixels):
+    """stbi_load(..., 4) channel expansion (icbc_test.cpp:345) of an (h, w, c)
+    or (h, w) uint8 array: grey -> (g, g, g, 255), grey + alpha -> (g, g, g, a),
+    RGB -> (r, g, b, 255), RGBA unchanged."""
+    p = np.asarray(pixels, np.uint8)
+    if p.ndim == 2:
+        p = p[:, :, None]
+    h, w, c = p.shape
+    out = np.empty((h, w, 4), np.uint8)
+    if c in (1, 2):
+        out[..., 0] = out[..., 1] = out[..., 2] = p[..., 0]
+    else:
+        out[..., :3] = p[..., :3]
+    out[..., 3] = p[..., c - 1] if c in (2, 4) else 255
+    return out
+
+
+def mip_down(rgba):
+    """One 2x2 box-filter mip step of an (h, w, 4) uint8 image: size
+    max(1, w >> 1) x max(1, h >> 1), each channel (a + b + c + d + 2) >> 2 over
+    texels (2x, 2y) .. (2x + 1, 2y + 1), coordinates clamped to the source."""
+    src = np.asarray(rgba, np.uint8).astype(np.int32)
+    h, w = src.shape[:2]
+    dh, dw = max(1, h >> 1), max(1, w >> 1)
+    xs0 = np.minimum(2 * np.arange(dw), w - 1)
+    xs1 = np.minimum(2 * np.arange(dw) + 1, w - 1)
+    ys0 = np.minimum(2 * np.arange(dh), h - 1)
+    ys1 = np.minimum(2 * np.arange(dh) + 1, h - 1)
+    s = (src[ys0][:, xs0] + src[ys0][:, xs1] + src[ys1][:, xs0] + src[ys1][:, xs1] + 2) >> 2
+    return s.astype(np.uint8)
+
+
+def mip_chain(rgba, levels=None):
+    """[level 0, level 1, ...] down to 1 x 1 (or `levels` levels)."""
+    out = [np.asarray(rgba, np.uint8)]
+    while (levels is None or len(out) < levels) and (out[-1].shape[0] > 1 or out[-1].shape[1] > 1):
+        out.append(mip_down(out[-1]))
+    return out

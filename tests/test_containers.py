@@ -60,3 +60,22 @@ def test_dds_from_device_blocks(gpu_lib, tmp_path):
     gpu_lib.write_dds(path, 96, 64, out)
     assert gpu_lib.compare_dds(path, 96, 64, out.cpu().numpy())
     assert gpu_lib.compare_dds(path, 96, 64, out)
+
+
+def test_dds_mip_chain_layout(tmp_path):
+    w, h = 37, 21
+    levels = ig.mip_levels(w, h)
+    assert levels == 6  # 37x21, 18x10, 9x5, 4x2, 2x1, 1x1
+    ws, hs, off = ig.mip_layout(w, h)
+    assert (ws, hs) == ([37, 18, 9, 4, 2, 1], [21, 10, 5, 2, 1, 1])
+    assert off == [0, 60, 75, 81, 82, 83, 84]
+    b = _blocks(100, 100)[: off[-1]]
+    path = str(tmp_path / "mips.dds")
+    ig.write_dds_mips(path, w, h, levels, b)
+    data = open(path, "rb").read()
+    assert len(data) == 128 + 8 * off[-1]
+    magic, size, flags, height, width, linear, depth, mips = struct.unpack("<4s7I", data[:32])
+    assert (magic, height, width, linear, mips) == (b"DDS ", h, w, 8 * off[1], levels)
+    assert flags & 0x20000  # DDSD_MIPMAPCOUNT
+    assert struct.unpack("<I", data[108:112])[0] == 0x1000 | 0x400000 | 0x8
+    assert data[128:] == b.tobytes()
