@@ -4,20 +4,24 @@
 //   * serial stages of icbc's compress_bc1 (reduce_colors, box fit, least
 //     squares, PCA + summed-area table, index selection, refinement) run one
 //     block per lane;
-//   * the 4- and 3-cluster enumerations (the hot loops) run cooperatively:
-//     the 32 lanes split one block's table of boundary combinations, keep the
-//     first strict minimum of their share and reduce with warp shuffles,
-//     ties going to the lowest table index -- the same winner the sequential
-//     loop of icbc.h:2362-2733 keeps.
+//   * the 4- and 3-cluster enumerations (the hot loops) run warp-wide: the
+//     combinations of every block of the warp that needs a search form one
+//     list, cut into 64 ranges walked two per lane; a walker keeps the first
+//     strict minimum of its share and folds it into its block's slot with a
+//     64-bit atomicMin, ties going to the lowest table index -- the winner
+//     the sequential loop of icbc.h:2362-2733 keeps.
 //
-// Shared memory per warp, [32 blocks][odd stride] so that per-lane rows are
-// conflict-free and one block's SAT can be read by all lanes at once:
-//   in    [32][65]  texels r,g,b (float) + weight, 16 x 4 floats
-//   sat   [32][69]  first the reduced colours + weights (reduce_colors, 16 x 4),
-//                   then, built in place through registers, the SAT with a
-//                   leading zero: component c at [c*17 + 0..16]
+// Shared memory per warp, one row per block of the warp:
+//   in    [32][65]  texels r,g,b (float) + weight, 16 x 4 floats (odd stride:
+//                   per-lane scalar accesses are conflict-free)
+//   sat   [32][68]  float4 (r, g, b, w) entries: first the reduced colours
+//                   (reduce_colors), then, built in place through registers,
+//                   the SAT with a leading zero entry, entries 0..16 (17
+//                   float4 per row: any 8 lanes' 16-byte accesses to entry k
+//                   of their rows, or to different entries of any rows in
+//                   the cluster search, spread over the 8 bank groups)
 //   slots [32]      u64 per block: best (error, table index) of a cluster search
-// The pad word [68] of each SAT row holds the block's search bookkeeping.
+//   info  [32]      int per block: its first combination | colour count << 16
 // 17 KB per warp: three 4-warp CTAs per SM at levels 2..9.
 #pragma once
 
@@ -27,11 +31,11 @@ namespace icbc_gpu {
 
 constexpr int kWarpsPerCta = 4;
 constexpr int kInStride = 65;
-constexpr int kSatStride = 69;
+constexpr int kSatStride = 68;
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr size_t kWarpFloatsLow = 32 * kInStride;                                  // L0, L1
-constexpr size_t kWarpFloatsHigh = 32 * kInStride + 32 * kSatStride + 64;         // L2..L9
+constexpr size_t kWarpFloatsHigh = 32 * kInStride + 32 * kSatStride + 64 + 32;    // L2..L9
 
 __host__ __device__ constexpr size_t smem_bytes(bool cluster_fit) {
     return sizeof(SharedTables) + kWarpsPerCta * 4 * (cluster_fit ? kWarpFloatsHigh : kWarpFloatsLow);
@@ -73,12 +77,21 @@ struct WarpCtx {
     const SharedTables *T;
     const DecoderTables *D;
     float *in;
-    float *sat;
-    unsigned long long *slots;
+    float *sat;                  // per block: 17 float4 (r, g, b, w) SAT entries
+    unsigned long long *slots;   // per block: the search's argmin key
+    int *info;                   // per block: first combination | count << 16
     int lane;
 };
 
 // ------------------------------------------------------------ per lane --
+
+// A lane's SAT row holds float4 (r, g, b, w) entries: its reduced colours,
+// then its summed-area table.  The row stride (17 float4) puts the 16-byte
+// accesses of 8 lanes (one shared-memory phase) in 8 different bank groups,
+// whether the lanes read their own rows or the walkers gather across rows.
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ V3 xyz(float4 v) { return v3(v.x, v.y, v.z); }
 
 // reduce_colors (icbc.h:1683-1728) into rrow (the lane's SAT row, as scratch).
 __device__ __forceinline__ int reduce_colors(const float *row, float threshold, float *rrow, bool &any_black) {
@@ -90,22 +103,18 @@ __device__ __forceinline__ int reduce_colors(const float *row, float threshold, 
         if (wi > 0) {
             int j = 0;
             for (; j < n; j++) {
-                const V3 cj = texel(rrow, j);
+                const float4 c4 = ld4(rrow + 4 * j);
+                const V3 cj = xyz(c4);
                 if (near3(cj, ci, threshold)) {
-                    const float wj = rrow[4 * j + 3];
+                    const float wj = c4.w;
                     const float s = wj + wi;
-                    rrow[4 * j + 0] = (cj.x * wj + ci.x * wi) / s;
-                    rrow[4 * j + 1] = (cj.y * wj + ci.y * wi) / s;
-                    rrow[4 * j + 2] = (cj.z * wj + ci.z * wi) / s;
-                    rrow[4 * j + 3] = s;
+                    st4(rrow + 4 * j, make_float4((cj.x * wj + ci.x * wi) / s, (cj.y * wj + ci.y * wi) / s,
+                                                  (cj.z * wj + ci.z * wi) / s, s));
                     break;
                 }
             }
             if (j == n) {
-                rrow[4 * n + 0] = ci.x;
-                rrow[4 * n + 1] = ci.y;
-                rrow[4 * n + 2] = ci.z;
-                rrow[4 * n + 3] = wi;
+                st4(rrow + 4 * n, make_float4(ci.x, ci.y, ci.z, wi));
                 n++;
             }
             if (is_black(ci)) any_black = true;
@@ -130,10 +139,11 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
 #pragma unroll
     for (int i = 0; i < 16; i++) {
         const bool in = i < count;
-        cx[i] = in ? srow[4 * i + 0] : 0.0f;
-        cy[i] = in ? srow[4 * i + 1] : 0.0f;
-        cz[i] = in ? srow[4 * i + 2] : 0.0f;
-        cw[i] = in ? srow[4 * i + 3] : 0.0f;
+        const float4 c = ld4(srow + 4 * i);
+        cx[i] = in ? c.x : 0.0f;
+        cy[i] = in ? c.y : 0.0f;
+        cz[i] = in ? c.z : 0.0f;
+        cw[i] = in ? c.w : 0.0f;
         if (in && !(skip_black && is_black(v3(cx[i], cy[i], cz[i])))) use |= 1u << i;
     }
     const int m = __popc(use);
@@ -180,8 +190,7 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
         dps[i] = dot(v3(cx[i], cy[i], cz[i]), axis);
         has_nan |= ((use >> i) & 1) && (dps[i] != dps[i]);
     }
-#pragma unroll
-    for (int c = 0; c < 4; c++) srow[c * 17] = 0.0f;
+    st4(srow, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     if (!has_nan) {
         // Stable ranks from the 120 pairs i < j: j sorts before i iff
         // dps[j] < dps[i]; otherwise i (the earlier one) sorts before j.
@@ -200,12 +209,7 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
         }
 #pragma unroll
         for (int i = 0; i < 16; i++) {
-            if (use & (1u << i)) {
-                srow[0 * 17 + pos[i] + 1] = cx[i] * cw[i];
-                srow[1 * 17 + pos[i] + 1] = cy[i] * cw[i];
-                srow[2 * 17 + pos[i] + 1] = cz[i] * cw[i];
-                srow[3 * 17 + pos[i] + 1] = cw[i];
-            }
+            if (use & (1u << i)) st4(srow + 4 * (pos[i] + 1), make_float4(cx[i] * cw[i], cy[i] * cw[i], cz[i] * cw[i], cw[i]));
         }
     } else {
         // Literal stable insertion sort of the kept colours (NaN keys).  The
@@ -232,15 +236,15 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
             }
         for (int q = 0; q < m; q++) {
             const float *c = lc + 4 * order[q];
-            srow[0 * 17 + q + 1] = c[0] * c[3];
-            srow[1 * 17 + q + 1] = c[1] * c[3];
-            srow[2 * 17 + q + 1] = c[2] * c[3];
-            srow[3 * 17 + q + 1] = c[3];
+            st4(srow + 4 * (q + 1), make_float4(c[0] * c[3], c[1] * c[3], c[2] * c[3], c[3]));
         }
     }
+    // Prefix sums in sorted order: entry k = entry k - 1 + term k.
+    float4 acc = ld4(srow + 4);
     for (int k = 2; k <= m; k++) {
-#pragma unroll
-        for (int c = 0; c < 4; c++) srow[c * 17 + k] = srow[c * 17 + k - 1] + srow[c * 17 + k];
+        const float4 t = ld4(srow + 4 * k);
+        acc = make_float4(acc.x + t.x, acc.y + t.y, acc.z + t.z, acc.w + t.w);
+        st4(srow + 4 * k, acc);
     }
     return m;
 }
@@ -294,11 +298,13 @@ __device__ __forceinline__ bool optimize_end_points4(const float *row, uint32_t 
 }
 
 // Box fit: fit_colors_bbox, inset_bbox, select_diagonal (icbc.h:3313-3368).
+// ROW4: `colors` is a SAT row (float4 entries); otherwise a texel row.
+template <bool ROW4>
 __device__ __forceinline__ void box_fit(const float *colors, int count, V3 &c0, V3 &c1) {
     c0 = v3(0.0f, 0.0f, 0.0f);
     c1 = v3(1.0f, 1.0f, 1.0f);
     for (int i = 0; i < count; i++) {
-        const V3 c = texel(colors, i);
+        const V3 c = ROW4 ? xyz(ld4(colors + 4 * i)) : texel(colors, i);
         c0 = vmax(c0, c);
         c1 = vmin(c1, c);
     }
@@ -310,7 +316,7 @@ __device__ __forceinline__ void box_fit(const float *colors, int count, V3 &c0, 
     const V3 center = (c0 + c1) * 0.5f;
     float cov_xz = 0.0f, cov_yz = 0.0f;
     for (int i = 0; i < count; i++) {
-        const V3 t = texel(colors, i) - center;
+        const V3 t = (ROW4 ? xyz(ld4(colors + 4 * i)) : texel(colors, i)) - center;
         cov_xz += t.x * t.z;
         cov_yz += t.y * t.z;
     }
@@ -456,11 +462,12 @@ struct FitWeights {
 };
 
 __device__ __forceinline__ FitSums fit_sums(const float *S, int count) {
+    const float4 v = ld4(S + 4 * count);
     FitSums k;
-    k.r_sum = S[0 * 17 + count];
-    k.g_sum = S[1 * 17 + count];
-    k.b_sum = S[2 * 17 + count];
-    k.w_sum = S[3 * 17 + count];
+    k.r_sum = v.x;
+    k.g_sum = v.y;
+    k.b_sum = v.z;
+    k.w_sum = v.w;
     return k;
 }
 
@@ -475,11 +482,10 @@ __device__ __forceinline__ FitWeights fit_weights(const DecoderTables *D, V3 met
 __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                           V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
-    V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
-    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
-    V3 x2 = v3(S[i2], S[17 + i2], S[34 + i2]);
-    const float w0 = S[51 + i0];
-    float w1 = S[51 + i1], w2 = S[51 + i2];
+    const float4 s0 = ld4(S + 4 * i0), s1 = ld4(S + 4 * i1), s2 = ld4(S + 4 * i2);
+    V3 x0 = xyz(s0), x1 = xyz(s1), x2 = xyz(s2);
+    const float w0 = s0.w;
+    float w1 = s1.w, w2 = s2.w;
     const float w3 = k.w_sum - w2;
     x2 = x2 - x1;
     x1 = x1 - x0;
@@ -508,10 +514,11 @@ __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, cons
 __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                           V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
-    const V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
-    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
-    const float w0 = S[51 + i0];
-    float w1 = S[51 + i1];
+    const float4 s0 = ld4(S + 4 * i0), s1 = ld4(S + 4 * i1);
+    const V3 x0 = xyz(s0);
+    V3 x1 = xyz(s1);
+    const float w0 = s0.w;
+    float w1 = s1.w;
     const float w2 = k.w_sum - w1;
     x1 = x1 - x0;
     w1 = w1 - w0;
@@ -563,11 +570,10 @@ __device__ __forceinline__ V3 pm_round_ept(V3 v, bool rne) {
 __device__ __forceinline__ float cf4_combo_simd(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                                bool f, bool rne, V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
-    V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
-    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
-    V3 x2 = v3(S[i2], S[17 + i2], S[34 + i2]);
-    const float w0 = S[51 + i0];
-    float w1 = S[51 + i1], w2 = S[51 + i2];
+    const float4 s0 = ld4(S + 4 * i0), s1 = ld4(S + 4 * i1), s2 = ld4(S + 4 * i2);
+    V3 x0 = xyz(s0), x1 = xyz(s1), x2 = xyz(s2);
+    const float w0 = s0.w;
+    float w1 = s1.w, w2 = s2.w;
     const float w3 = k.w_sum - w2;
     x2 = x2 - x1;
     x1 = x1 - x0;
@@ -598,10 +604,11 @@ __device__ __forceinline__ float cf4_combo_simd(const float *S, uint32_t packed,
 __device__ __forceinline__ float cf3_combo_simd(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                                bool f, bool rne, V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
-    const V3 x0 = v3(S[i0], S[17 + i0], S[34 + i0]);
-    V3 x1 = v3(S[i1], S[17 + i1], S[34 + i1]);
-    const float w0 = S[51 + i0];
-    float w1 = S[51 + i1];
+    const float4 s0 = ld4(S + 4 * i0), s1 = ld4(S + 4 * i1);
+    const V3 x0 = xyz(s0);
+    V3 x1 = xyz(s1);
+    const float w0 = s0.w;
+    float w1 = s1.w;
     const float w2 = k.w_sum - w1;
     x1 = x1 - x0;
     w1 = w1 - w0;
@@ -627,10 +634,7 @@ __device__ __forceinline__ float cf3_combo_simd(const float *S, uint32_t packed,
 // compute_sat's FLT_MAX fill of the entries past the colour count
 // (icbc.h:1931-1936), which the SIMD loops read for their padding lanes.
 __device__ __forceinline__ void fill_sat_tail(float *srow, int m) {
-    for (int k = m + 1; k <= 16; k++) {
-#pragma unroll
-        for (int c = 0; c < 4; c++) srow[c * 17 + k] = FLT_MAX;
-    }
+    for (int k = m + 1; k <= 16; k++) st4(srow + 4 * k, make_float4(FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX));
 }
 
 // In a SIMD build, combination k of a block is evaluated in lane k % vec;
@@ -661,7 +665,7 @@ struct Walker {
     int best_k;
 };
 
-__device__ __forceinline__ int block_info(const WarpCtx &w, int b) { return __float_as_int(w.sat[b * kSatStride + 68]); }
+__device__ __forceinline__ int block_info(const WarpCtx &w, int b) { return w.info[b]; }
 
 // With SIMD, a block's combinations run to a whole number of vectors of
 // `vec` lanes (icbc.h:2089, :2362: the padding lanes read table entries of
@@ -671,7 +675,7 @@ __device__ __forceinline__ int padded_total(int t, int vec) { return (t + vec - 
 template <bool FOUR, bool SIMD = false>
 __device__ __forceinline__ void walker_enter(const WarpCtx &w, Walker &v, int b, int k, int vec = 1) {
     const float *S = w.sat + b * kSatStride;
-    const int cnt = __float_as_int(S[68]) >> 16;
+    const int cnt = w.info[b] >> 16;
     v.b = b;
     v.k = k;
     v.S = S;
@@ -761,7 +765,7 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
         if (lane >= off) incl += y;
     }
     const int W = __shfl_sync(kFull, incl, 31);
-    w.sat[lane * kSatStride + 68] = __int_as_float((incl - T) | ((need ? count : 0) << 16));
+    w.info[lane] = (incl - T) | ((need ? count : 0) << 16);
     w.slots[lane] = ~0ull;
     __syncwarp();
     if (W == 0) return -1;
@@ -829,14 +833,14 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
             c0 = c1 = idx = 0;
             err = 0.0f;
         } else if (O::cluster && count == 1) {
-            single_color(w.D, texel(srow, 0), c0, c1, idx);
+            single_color(w.D, xyz(ld4(srow)), c0, c1, idx);
             err = block_error(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D), idx);
         } else {
             live = true;
             err = FLT_MAX;
             if (O::box) {
                 V3 e0, e1;
-                box_fit(O::cluster ? srow : row, count, e0, e1);
+                box_fit<O::cluster>(O::cluster ? srow : row, count, e0, e1);
                 err = output_block4(w, row, p, e0, e1, c0, c1, idx);
                 if (O::lsq && optimize_end_points4(row, idx, e0, e1)) {
                     uint32_t o0, o1, oi;

@@ -92,6 +92,7 @@ __device__ __forceinline__ WarpCtx warp_ctx(unsigned char *smem, const SharedTab
     w.in = base;
     w.sat = base + 32 * kInStride;
     w.slots = reinterpret_cast<unsigned long long *>(base + 32 * kInStride + 32 * kSatStride);
+    w.info = reinterpret_cast<int *>(base + 32 * kInStride + 32 * kSatStride + 64);
     w.lane = threadIdx.x & 31;
     return w;
 }
