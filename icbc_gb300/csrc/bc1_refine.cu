@@ -42,6 +42,8 @@ __device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_
     }
 }
 
+constexpr int kRefillBatch = 8;
+
 // MODE 0: float blocks (s), 1: one image (d), 2: the deferred level-9 blocks
 // of a batch (images + map), each lane with its own image's decoder and
 // parameters.
@@ -65,7 +67,11 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
     for (;;) {
         // Lanes without a block take the next ones; blocks that need no
         // refinement are skipped (their error and bytes are final already).
+        // Refills run in batches: a lane that finished waits until
+        // kRefillBatch lanes (or all) need a block, so the divergent refill
+        // code runs for many lanes at once instead of one at a time.
         unsigned need = __ballot_sync(kFull, !have && !exhausted);
+        if (__popc(need) < kRefillBatch && __any_sync(kFull, have)) need = 0;
         while (need) {
             const int leader = __ffs(need) - 1;
             unsigned long long base = 0;
