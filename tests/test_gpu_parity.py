@@ -234,6 +234,31 @@ def test_batch_with_own_launch_images(gpu_lib):
     batch.close()
 
 
+def test_host_buffer_path_in_bands(gpu_lib):
+    """Images of 128+ block rows go through the host path in bands (copies
+    of one band overlapping the encode of another); results equal the device
+    path and the oracle, weight planes and level 4+ prior output included."""
+    import torch
+    ig = gpu_lib
+    w, h = 1030, 602  # 151 block rows: 2 bands, the last one with a partial block row
+    img = synth.quality_sweep_image(w, h, seed=21)
+    plane = np.random.default_rng(3).random((h, w), dtype=np.float32)
+    dev = _to_dev(img)
+    dplane = torch.from_numpy(plane).cuda()
+    nb = ig.blocks_of(w, h)
+    for level, wm in ((9, ig.WEIGHTS_ALPHA), (8, ig.WEIGHTS_ALPHA), (4, ig.WEIGHTS_PLANE), (1, ig.WEIGHTS_UNIFORM)):
+        errs = np.zeros(nb, np.float32)
+        out = ig.compress_image_host(img, level, 1, (0.299, 0.587, 0.114), wm, errors=errs,
+                                     weight_plane=plane if wm == ig.WEIGHTS_PLANE else None)
+        db, de = ig.compress_image(dev, level, 1, (0.299, 0.587, 0.114), wm,
+                                   dplane if wm == ig.WEIGHTS_PLANE else None, with_errors=True)
+        assert np.array_equal(out, db.cpu().numpy()), level
+        assert same_bits(errs, de.cpu().numpy()), level
+        if level == 8:
+            ob, oe = O.encode_image(img, level, 1, (0.299, 0.587, 0.114), 1, None, True, True, nthreads=16)
+            assert np.array_equal(out, ob) and same_bits(errs, oe)
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib
