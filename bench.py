@@ -57,6 +57,15 @@ OPS_PER_UNIT = {
 REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
 
 
+# DRAM bytes per level call (dram__bytes_read.sum + dram__bytes_write.sum of
+# its launches) from one ncu capture of this workload, summarised in
+# profiles/k_encode_image_L8_L9_k_refine_quality_sweep_4096.md.  Level 9 is
+# the encoder plus the refinement pass; each reads the 64 MB image.
+NCU_TRAFFIC_BYTES = {8: 75.61e6 + 0.85e6, 9: (75.68e6 + 2.82e6) + (76.00e6 + 2.16e6)}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum per level call, " \
+                 "profiles/k_encode_image_L8_L9_k_refine_quality_sweep_4096.md"
+
+
 def algorithmic_ops(stats: dict, level: int) -> float:
     ops = sum(OPS_PER_UNIT[k] * stats.get(k, 0) for k in OPS_PER_UNIT)
     if level >= 2:
@@ -337,7 +346,8 @@ def run_ours(args):
         "per_level": per_level,
         "mismatches_sampled": mismatches,
         "roofline": {"bound": "fp32", "kernel": "k_encode_image<%d>" % top, "achieved": achieved, "peak": peak,
-                     "unit": "Tops/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "Tops/s", "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES.get(top),
+                     "traffic_unit": "bytes per level call", "traffic_source": TRAFFIC_SOURCE,
                      "peak_source": "128 FP32 lanes x %d SMs x %s MHz (%s sm_max_mhz)" % (
                          sms, peaks.get("sm_max_mhz"), peaks["source"])},
         "roofline_hbm_level0": ({"bound": "hbm", "achieved": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9, "peak": hbm,
