@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
             case 7: e = encode_warp<7>(w, p, active, c0, c1, idx); break;
             case 8: e = encode_warp<8>(w, p, active, c0, c1, idx); break;
             default:
-                if (base >= 0) e = encode_warp_ex<9, true>(w, p, active, c0, c1, idx, pending);
+                if (base >= 0) e = encode_warp_ex<9, true>(w, float_row(w), p, active, c0, c1, idx, pending);
                 else e = encode_warp<9>(w, p, active, c0, c1, idx);
                 break;
         }

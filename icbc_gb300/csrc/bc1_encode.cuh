@@ -40,6 +40,12 @@ constexpr size_t kWarpFloatsHigh = 32 * kInStride + 32 * kSatStride + 64 + 32;  
 __host__ __device__ constexpr size_t smem_bytes(bool cluster_fit) {
     return sizeof(SharedTables) + kWarpsPerCta * 4 * (cluster_fit ? kWarpFloatsHigh : kWarpFloatsLow);
 }
+// The RGBA8 image kernels of levels 2..9 keep texels as bytes (ByteRow): 17
+// words per lane (odd stride) instead of 65 floats, 11 KB per warp in all --
+// small enough for four CTAs per SM.
+constexpr int kInWordsByte = 17;
+constexpr size_t kWarpFloatsByte = 32 * kInWordsByte + 32 * kSatStride + 64 + 32;
+__host__ __device__ constexpr size_t smem_bytes_byte_rows() { return sizeof(SharedTables) + kWarpsPerCta * 4 * kWarpFloatsByte; }
 
 // Options of each quality level (setup_options, icbc.h:3663-3731).
 template <int L>
@@ -94,12 +100,13 @@ __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<floa
 __device__ __forceinline__ V3 xyz(float4 v) { return v3(v.x, v.y, v.z); }
 
 // reduce_colors (icbc.h:1683-1728) into rrow (the lane's SAT row, as scratch).
-__device__ __forceinline__ int reduce_colors(const float *row, float threshold, float *rrow, bool &any_black) {
+template <class Row>
+__device__ __forceinline__ int reduce_colors(const Row &row, float threshold, float *rrow, bool &any_black) {
     int n = 0;
     any_black = false;
     for (int i = 0; i < 16; i++) {
-        const V3 ci = texel(row, i);
-        const float wi = row[4 * i + 3];
+        const V3 ci = row.color(i);
+        const float wi = row.weight(i);
         if (wi > 0) {
             int j = 0;
             for (; j < n; j++) {
@@ -250,7 +257,8 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
 }
 
 // output_block4 (icbc.h:3257-3274): endpoints ordered col0 >= col1.
-__device__ __forceinline__ float output_block4(const WarpCtx &w, const float *row, const EncodeParams &p, V3 v0, V3 v1,
+template <class Row>
+__device__ __forceinline__ float output_block4(const WarpCtx &w, const Row &row, const EncodeParams &p, V3 v0, V3 v1,
                                                uint32_t &c0, uint32_t &c1, uint32_t &idx) {
     uint32_t a = to565(v0, *w.T), b = to565(v1, *w.T);
     if (a < b) { const uint32_t t = a; a = b; b = t; }
@@ -261,7 +269,8 @@ __device__ __forceinline__ float output_block4(const WarpCtx &w, const float *ro
 }
 
 // output_block3 (icbc.h:3238-3255): endpoints ordered col0 <= col1.
-__device__ __forceinline__ float output_block3(const WarpCtx &w, const float *row, const EncodeParams &p, V3 v0, V3 v1,
+template <class Row>
+__device__ __forceinline__ float output_block3(const WarpCtx &w, const Row &row, const EncodeParams &p, V3 v0, V3 v1,
                                                uint32_t &c0, uint32_t &c1, uint32_t &idx) {
     uint32_t a = to565(v0, *w.T), b = to565(v1, *w.T);
     if (a > b) { const uint32_t t = a; a = b; b = t; }
@@ -273,7 +282,8 @@ __device__ __forceinline__ float output_block3(const WarpCtx &w, const float *ro
 
 // optimize_end_points4 (icbc.h:3278-3310): unweighted least squares over the
 // 16 input texels for fixed indices.
-__device__ __forceinline__ bool optimize_end_points4(const float *row, uint32_t indices, V3 &a, V3 &b) {
+template <class Row>
+__device__ __forceinline__ bool optimize_end_points4(const Row &row, uint32_t indices, V3 &a, V3 &b) {
     float alpha2 = 0.0f, beta2 = 0.0f, ab = 0.0f;
     V3 ax = v3(0.0f, 0.0f, 0.0f), bx = v3(0.0f, 0.0f, 0.0f);
 #pragma unroll 1
@@ -285,7 +295,7 @@ __device__ __forceinline__ bool optimize_end_points4(const float *row, uint32_t 
         alpha2 += alpha * alpha;
         beta2 += beta * beta;
         ab += alpha * beta;
-        const V3 c = texel(row, i);
+        const V3 c = row.color(i);
         ax = ax + c * alpha;
         bx = bx + c * beta;
     }
@@ -298,13 +308,18 @@ __device__ __forceinline__ bool optimize_end_points4(const float *row, uint32_t 
 }
 
 // Box fit: fit_colors_bbox, inset_bbox, select_diagonal (icbc.h:3313-3368).
-// ROW4: `colors` is a SAT row (float4 entries); otherwise a texel row.
-template <bool ROW4>
-__device__ __forceinline__ void box_fit(const float *colors, int count, V3 &c0, V3 &c1) {
+// `colors`: the reduced colours in a SAT row (SatColors) or a texel row.
+struct SatColors {
+    const float *p;
+    __device__ __forceinline__ V3 color(int i) const { return xyz(ld4(p + 4 * i)); }
+};
+
+template <class C>
+__device__ __forceinline__ void box_fit(const C &colors, int count, V3 &c0, V3 &c1) {
     c0 = v3(0.0f, 0.0f, 0.0f);
     c1 = v3(1.0f, 1.0f, 1.0f);
     for (int i = 0; i < count; i++) {
-        const V3 c = ROW4 ? xyz(ld4(colors + 4 * i)) : texel(colors, i);
+        const V3 c = colors.color(i);
         c0 = vmax(c0, c);
         c1 = vmin(c1, c);
     }
@@ -316,7 +331,7 @@ __device__ __forceinline__ void box_fit(const float *colors, int count, V3 &c0, 
     const V3 center = (c0 + c1) * 0.5f;
     float cov_xz = 0.0f, cov_yz = 0.0f;
     for (int i = 0; i < count; i++) {
-        const V3 t = (ROW4 ? xyz(ld4(colors + 4 * i)) : texel(colors, i)) - center;
+        const V3 t = colors.color(i) - center;
         cov_xz += t.x * t.z;
         cov_yz += t.y * t.z;
     }
@@ -349,13 +364,13 @@ __device__ __forceinline__ uint32_t add565(uint32_t c, int dr, int dg, int db) {
 }
 
 // Generic nearest-of-four indices (compute_indices, icbc.h:3179-3235).
-template <int UNROLL = 1>
-__device__ __forceinline__ uint32_t indices_generic(const float *row, V3 cw, const PalF &pal) {
+template <int UNROLL = 1, class Row>
+__device__ __forceinline__ uint32_t indices_generic(const Row &row, V3 cw, const PalF &pal) {
     const V3 p0 = pal.c[0] * cw, p1 = pal.c[1] * cw, p2 = pal.c[2] * cw, p3 = pal.c[3] * cw;
     uint32_t out = 0;
 #pragma unroll UNROLL
     for (int t = 0; t < 16; t++) {
-        const V3 c = texel(row, t) * cw;
+        const V3 c = row.color(t) * cw;
         const V3 t0 = c - p0, t1 = c - p1, t2 = c - p2, t3 = c - p3;
         const float d0 = dot(t0, t0), d1 = dot(t1, t1), d2 = dot(t2, t2), d3 = dot(t3, t3);
         const bool i1 = (d1 <= d0) & (d1 < d2) & (d1 < d3);
@@ -369,7 +384,8 @@ __device__ __forceinline__ uint32_t indices_generic(const float *row, V3 cw, con
 // refine_endpoints (icbc.h:3574-3651).  Indices of a step come from the
 // palette of the current best block, so they change only when a step is
 // accepted; the step's error uses the moved endpoints' palette.
-__device__ __forceinline__ float refine(const WarpCtx &w, const float *row, const EncodeParams &p, float input_error,
+template <class Row>
+__device__ __forceinline__ float refine(const WarpCtx &w, const Row &row, const EncodeParams &p, float input_error,
                                         uint32_t &c0, uint32_t &c1, uint32_t &idx) {
     float best = input_error;
     int last = 0;
@@ -406,7 +422,8 @@ struct RefineLane {
     int i, last;
 };
 
-__device__ __forceinline__ void refine_begin(const WarpCtx &w, const float *row, const EncodeParams &p, float error,
+template <class Row>
+__device__ __forceinline__ void refine_begin(const WarpCtx &w, const Row &row, const EncodeParams &p, float error,
                                              uint32_t c0, uint32_t c1, uint32_t idx, RefineLane &s) {
     s.c0 = c0;
     s.c1 = c1;
@@ -419,7 +436,8 @@ __device__ __forceinline__ void refine_begin(const WarpCtx &w, const float *row,
 
 // Iteration s.i of refine_endpoints (icbc.h:3614-3648), identical to one trip
 // of refine()'s loop.  Returns true when the loop would stop after it.
-__device__ __forceinline__ bool refine_step(const WarpCtx &w, const float *row, const EncodeParams &p, RefineLane &s) {
+template <class Row>
+__device__ __forceinline__ bool refine_step(const WarpCtx &w, const Row &row, const EncodeParams &p, RefineLane &s) {
     const int d = s.i & 15;
     const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
     uint32_t r0 = s.c0, r1 = s.c1;
@@ -815,13 +833,14 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 // With DEFER the refinement of level 9 is not run here: `refine_next` is set
 // for the blocks it applies to (the caller hands them to k_refine), and the
 // returned error is the one refinement starts from.
-template <int L, bool DEFER, bool SIMD = false>
-__device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
-                                                uint32_t &c1, uint32_t &idx, bool &refine_next) {
+__device__ __forceinline__ FloatRow float_row(const WarpCtx &w) { return FloatRow{w.in + w.lane * kInStride}; }
+
+template <int L, bool DEFER, bool SIMD = false, class Row>
+__device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row, const EncodeParams &p, bool active,
+                                                uint32_t &c0, uint32_t &c1, uint32_t &idx, bool &refine_next) {
     using O = Level<L>;
     refine_next = false;
     const int lane = w.lane;
-    const float *row = w.in + lane * kInStride;
     float *srow = w.sat + lane * kSatStride;
     float err = 0.0f;
     int count = 16;
@@ -840,7 +859,8 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
             err = FLT_MAX;
             if (O::box) {
                 V3 e0, e1;
-                box_fit<O::cluster>(O::cluster ? srow : row, count, e0, e1);
+                if (O::cluster) box_fit(SatColors{srow}, count, e0, e1);
+                else box_fit(row, count, e0, e1);
                 err = output_block4(w, row, p, e0, e1, c0, c1, idx);
                 if (O::lsq && optimize_end_points4(row, idx, e0, e1)) {
                     uint32_t o0, o1, oi;
@@ -912,11 +932,12 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const EncodePa
     return err;
 }
 
+// encode_warp_ex on the warp's float texel rows, refinement inline.
 template <int L>
 __device__ __forceinline__ float encode_warp(const WarpCtx &w, const EncodeParams &p, bool active, uint32_t &c0,
                                              uint32_t &c1, uint32_t &idx) {
     bool unused;
-    return encode_warp_ex<L, false>(w, p, active, c0, c1, idx, unused);
+    return encode_warp_ex<L, false>(w, float_row(w), p, active, c0, c1, idx, unused);
 }
 
 }  // namespace icbc_gpu

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_blocks(const Globa
             idx = prev.y;
         }
         bool pending;
-        const float e = encode_warp_ex<L, DEFER>(w, p, active, c0, c1, idx, pending);
+        const float e = encode_warp_ex<L, DEFER>(w, float_row(w), p, active, c0, c1, idx, pending);
         if (active) {
             out[b] = make_uint2(c0 | (c1 << 16), idx);
             if (errors) errors[b] = e;
@@ -75,7 +75,43 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_image(const Global
             idx = prev.y;
         }
         bool pending;
-        const float e = encode_warp_ex<L, DEFER>(w, p, active, c0, c1, idx, pending);
+        const float e = encode_warp_ex<L, DEFER>(w, float_row(w), p, active, c0, c1, idx, pending);
+        if (active) {
+            d.out[b] = make_uint2(c0 | (c1 << 16), idx);
+            if (d.errors) d.errors[b] = e;
+            if (DEFER) st[b] = RefineSlot{e, pending ? 1u : 0u};
+        }
+    }
+}
+
+// k_encode_image with byte texel rows, for RGBA8 images with uniform or alpha
+// weights at levels 2..9: 11 KB of shared memory per warp and at most 128
+// registers per thread, so four CTAs (16 warps) fit on an SM instead of three.
+template <int L, bool DEFER>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_encode_image_bytes(const GlobalTables *G, ImageDesc d,
+                                                                             EncodeParams p, RefineSlot *st) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    const WarpCtx w = warp_ctx_byte_rows(smem, T, G, p.decoder);
+    const ByteRow row = byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA);
+    const int64_t groups = (d.nblocks + 31) / 32;
+    for (int64_t g = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); g < groups;
+         g += (int64_t)gridDim.x * kWarpsPerCta) {
+        const int64_t b = g * 32 + w.lane;
+        const bool active = b < d.nblocks;
+        __syncwarp();
+        if (active) load_image_block_bytes(d, b, reinterpret_cast<uint32_t *>(w.in) + w.lane * kInWordsByte);
+        __syncwarp();
+        uint32_t c0 = 0, c1 = 0, idx = 0;
+        if (L >= 4 && active) {
+            const uint2 prev = d.out[b];
+            c0 = prev.x & 0xffff;
+            c1 = prev.x >> 16;
+            idx = prev.y;
+        }
+        bool pending;
+        const float e = encode_warp_ex<L, DEFER>(w, row, p, active, c0, c1, idx, pending);
         if (active) {
             d.out[b] = make_uint2(c0 | (c1 << 16), idx);
             if (d.errors) d.errors[b] = e;
@@ -92,17 +128,16 @@ constexpr int L = ICBC_LEVEL;
 // otherwise there are enough CTAs for the work and the hardware balances
 // them (better when block costs vary, as they do from level 2 on).
 template <class K>
-static int grid_for(K kernel, int64_t n, int sms) {
+static int grid_for(K kernel, int64_t n, int sms, size_t smem, int &resident) {
     const LaunchShape shape = launch_shape(L);
     const int64_t groups = (n + 31) / 32;
     const int64_t per_cta = (int64_t)kWarpsPerCta * shape.groups_per_warp;
     int64_t ctas = (groups + per_cta - 1) / per_cta;
     if (shape.persistent) {
-        static int resident = 0;
         if (!resident) {
             int per_sm = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerCta * 32,
-                                                              smem_bytes(Level<L>::cluster)) != cudaSuccess ||
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerCta * 32, smem) !=
+                    cudaSuccess ||
                 per_sm < 1)
                 per_sm = 1;
             resident = per_sm;
@@ -126,14 +161,13 @@ constexpr bool kDefer = Level<L>::refine;
 // `ext_st` (n slots) and `ext_counter` when given (graph captures, where
 // nothing is allocated).
 template <class Kernel, class Launch>
-static cudaError_t run(Kernel kernel, int64_t n, int sms, cudaStream_t stream, Launch launch,
-                       const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks, const EncodeParams &p,
-                       uint2 *out, float *errors, RefineSlot *ext_st = nullptr,
+static cudaError_t run(Kernel kernel, size_t smem, int &resident, int64_t n, int sms, cudaStream_t stream,
+                       Launch launch, const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
+                       const EncodeParams &p, uint2 *out, float *errors, RefineSlot *ext_st = nullptr,
                        unsigned long long *ext_counter = nullptr) {
-    const size_t smem = smem_bytes(Level<L>::cluster);
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int grid = grid_for(kernel, n, sms);
+    const int grid = grid_for(kernel, n, sms, smem, resident);
     if (!kDefer) {
         launch(grid, smem, nullptr);
         return cudaGetLastError();
@@ -159,10 +193,35 @@ static cudaError_t run(Kernel kernel, int64_t n, int sms, cudaStream_t stream, L
     return e != cudaSuccess ? e : f;
 }
 
+// Resident CTAs per SM of each kernel (persistent launch shapes), found once.
+static int g_resident_blocks = 0, g_resident_image = 0, g_resident_bytes = 0;
+
+// Byte rows apply to the cluster-fit levels and to RGBA8 weights (uniform or
+// alpha); weight planes need float rows.
+static bool use_byte_rows(const ImageDesc &d) { return Level<L>::cluster && d.weight_mode != ICBC_GPU_WEIGHTS_PLANE; }
+
+static cudaError_t launch_image(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p, cudaStream_t stream,
+                                int sms, RefineSlot *ext_st, unsigned long long *ext_counter) {
+    if constexpr (Level<L>::cluster) {
+        if (use_byte_rows(d))
+            return run(k_encode_image_bytes<L, kDefer>, smem_bytes_byte_rows(), g_resident_bytes, d.nblocks, sms,
+                       stream,
+                       [&](int grid, size_t smem, RefineSlot *slots) {
+                           k_encode_image_bytes<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, slots);
+                       },
+                       G, &d, nullptr, p, d.out, d.errors, ext_st, ext_counter);
+    }
+    return run(k_encode_image<L, kDefer>, smem_bytes(Level<L>::cluster), g_resident_image, d.nblocks, sms, stream,
+               [&](int grid, size_t smem, RefineSlot *slots) {
+                   k_encode_image<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, slots);
+               },
+               G, &d, nullptr, p, d.out, d.errors, ext_st, ext_counter);
+}
+
 cudaError_t ICBC_CAT(launch_blocks_l, ICBC_LEVEL)(const GlobalTables *G, const BlocksSrc &s, const EncodeParams &p,
                                                   void *out, float *errors, int64_t n, cudaStream_t stream, int sms) {
     uint2 *o = reinterpret_cast<uint2 *>(out);
-    return run(k_encode_blocks<L, kDefer>, n, sms, stream,
+    return run(k_encode_blocks<L, kDefer>, smem_bytes(Level<L>::cluster), g_resident_blocks, n, sms, stream,
                [&](int grid, size_t smem, RefineSlot *st) {
                    k_encode_blocks<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, s, p, o, errors, n, st);
                },
@@ -171,11 +230,7 @@ cudaError_t ICBC_CAT(launch_blocks_l, ICBC_LEVEL)(const GlobalTables *G, const B
 
 cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
                                                  cudaStream_t stream, int sms) {
-    return run(k_encode_image<L, kDefer>, d.nblocks, sms, stream,
-               [&](int grid, size_t smem, RefineSlot *st) {
-                   k_encode_image<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, st);
-               },
-               G, &d, nullptr, p, d.out, d.errors);
+    return launch_image(G, d, p, stream, sms, nullptr, nullptr);
 }
 
 // As launch_image_l<L>, with level 9's hand-over in the caller's memory
@@ -183,11 +238,7 @@ cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const Im
 cudaError_t ICBC_CAT(launch_image_ext_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
                                                      cudaStream_t stream, int sms, RefineSlot *st,
                                                      unsigned long long *counter) {
-    return run(k_encode_image<L, kDefer>, d.nblocks, sms, stream,
-               [&](int grid, size_t smem, RefineSlot *slots) {
-                   k_encode_image<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, slots);
-               },
-               G, &d, nullptr, p, d.out, d.errors, st, counter);
+    return launch_image(G, d, p, stream, sms, st, counter);
 }
 
 }  // namespace icbc_gpu

@@ -35,13 +35,12 @@ __device__ __forceinline__ void load_float_blocks(const BlocksSrc &s, int64_t ba
     }
 }
 
-// One block of an RGBA8 image into this lane's row: four 16-byte row loads
-// when the block is whole and rows are 16-byte aligned, else clamped texel
-// loads (edge replication).  u8 -> float is the exact table of i / 255.0f.
-__device__ __forceinline__ void load_image_block(const ImageDesc &d, int64_t b, float *row, const float *lut) {
+// The 16 RGBA8 texels of block b of an image: four 16-byte row loads when
+// the block is whole and rows are 16-byte aligned, else clamped texel loads
+// (edge replication).
+__device__ __forceinline__ void fetch_image_block(const ImageDesc &d, int64_t b, uint32_t px[16]) {
     const int bx = (int)(b % d.bw), by = (int)(b / d.bw);
     const int x0 = bx * 4, y0 = by * 4;
-    uint32_t px[16];
     if (d.vec16 && x0 + 4 <= d.width && y0 + 4 <= d.height) {
 #pragma unroll
         for (int r = 0; r < 4; r++) {
@@ -58,6 +57,15 @@ __device__ __forceinline__ void load_image_block(const ImageDesc &d, int64_t b, 
             px[t] = __ldg(reinterpret_cast<const uint32_t *>(d.rgba + (int64_t)y * d.pitch) + x);
         }
     }
+}
+
+// One block of an RGBA8 image into this lane's float row.  u8 -> float is
+// the exact table of i / 255.0f.
+__device__ __forceinline__ void load_image_block(const ImageDesc &d, int64_t b, float *row, const float *lut) {
+    const int bx = (int)(b % d.bw), by = (int)(b / d.bw);
+    const int x0 = bx * 4, y0 = by * 4;
+    uint32_t px[16];
+    fetch_image_block(d, b, px);
 #pragma unroll
     for (int t = 0; t < 16; t++) {
         row[4 * t + 0] = lut[px[t] & 255];
@@ -72,6 +80,14 @@ __device__ __forceinline__ void load_image_block(const ImageDesc &d, int64_t b, 
         }
         row[4 * t + 3] = w;
     }
+}
+
+// One block of an RGBA8 image into this lane's byte row (the words as they are).
+__device__ __forceinline__ void load_image_block_bytes(const ImageDesc &d, int64_t b, uint32_t *row) {
+    uint32_t px[16];
+    fetch_image_block(d, b, px);
+#pragma unroll
+    for (int t = 0; t < 16; t++) row[t] = px[t];
 }
 
 __device__ __forceinline__ void stage_tables(SharedTables &T, const GlobalTables *G) {
@@ -95,6 +111,27 @@ __device__ __forceinline__ WarpCtx warp_ctx(unsigned char *smem, const SharedTab
     w.info = reinterpret_cast<int *>(base + 32 * kInStride + 32 * kSatStride + 64);
     w.lane = threadIdx.x & 31;
     return w;
+}
+
+// The warp's context with byte texel rows (levels 2..9): w.in holds 32 rows
+// of kInWordsByte words.
+__device__ __forceinline__ WarpCtx warp_ctx_byte_rows(unsigned char *smem, const SharedTables &T, const GlobalTables *G,
+                                                      int decoder) {
+    const int warp = threadIdx.x >> 5;
+    float *base = reinterpret_cast<float *>(smem + sizeof(SharedTables)) + warp * kWarpFloatsByte;
+    WarpCtx w;
+    w.T = &T;
+    w.D = &G->dec[decoder];
+    w.in = base;
+    w.sat = base + 32 * kInWordsByte;
+    w.slots = reinterpret_cast<unsigned long long *>(base + 32 * kInWordsByte + 32 * kSatStride);
+    w.info = reinterpret_cast<int *>(base + 32 * kInWordsByte + 32 * kSatStride + 64);
+    w.lane = threadIdx.x & 31;
+    return w;
+}
+
+__device__ __forceinline__ ByteRow byte_row(const WarpCtx &w, int alpha) {
+    return ByteRow{reinterpret_cast<const uint32_t *>(w.in) + w.lane * kInWordsByte, w.T->lut255, alpha};
 }
 
 }  // namespace icbc_gpu

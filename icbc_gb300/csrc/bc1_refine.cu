@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
                             er = errors ? errors + mine : nullptr;
                         }
                         const uint2 cur = *o;
-                        refine_begin(w, row, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
+                        refine_begin(w, FloatRow{row}, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
                         have = true;
                     }
                 }
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
             need = __ballot_sync(kFull, !have && !exhausted);
         }
         if (!__any_sync(kFull, have)) break;
-        if (have && refine_step(w, row, lp, r)) {
+        if (have && refine_step(w, FloatRow{row}, lp, r)) {
             *o = make_uint2(r.c0 | (r.c1 << 16), r.idx);
             if (er) *er = r.best;
             have = false;

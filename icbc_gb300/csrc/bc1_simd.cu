@@ -45,14 +45,14 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_simd(const GlobalT
         bool unused;
         float e = 0.0f;
         switch (level) {
-            case 2: e = encode_warp_ex<2, false, true>(w, p, active, c0, c1, idx, unused); break;
-            case 3: e = encode_warp_ex<3, false, true>(w, p, active, c0, c1, idx, unused); break;
-            case 4: e = encode_warp_ex<4, false, true>(w, p, active, c0, c1, idx, unused); break;
-            case 5: e = encode_warp_ex<5, false, true>(w, p, active, c0, c1, idx, unused); break;
-            case 6: e = encode_warp_ex<6, false, true>(w, p, active, c0, c1, idx, unused); break;
-            case 7: e = encode_warp_ex<7, false, true>(w, p, active, c0, c1, idx, unused); break;
-            case 8: e = encode_warp_ex<8, false, true>(w, p, active, c0, c1, idx, unused); break;
-            default: e = encode_warp_ex<9, false, true>(w, p, active, c0, c1, idx, unused); break;
+            case 2: e = encode_warp_ex<2, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            case 3: e = encode_warp_ex<3, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            case 4: e = encode_warp_ex<4, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            case 5: e = encode_warp_ex<5, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            case 6: e = encode_warp_ex<6, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            case 7: e = encode_warp_ex<7, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            case 8: e = encode_warp_ex<8, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
+            default: e = encode_warp_ex<9, false, true>(w, float_row(w), p, active, c0, c1, idx, unused); break;
         }
         if (active) {
             out[b] = make_uint2(c0 | (c1 << 16), idx);
