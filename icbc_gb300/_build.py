@@ -36,8 +36,8 @@ def nvcc() -> str:
 def _units():
     """(source, extra flags, object name) of every translation unit."""
     # The all-levels units (batch, SIMD profiles, no-alloc) compile longest: start them first.
-    units = [(os.path.join(CSRC, n), [], n.replace(".cu", ".o"))
-             for n in ("bc1_batch.cu", "bc1_simd.cu", "bc1_noalloc.cu")]
+    units = [(os.path.join(CSRC, "bc1_batch.cu"), ["-DICBC_BATCH_BYTES=%d" % v], "bc1_batch%d.o" % v) for v in (1, 0)]
+    units += [(os.path.join(CSRC, n), [], n.replace(".cu", ".o")) for n in ("bc1_simd.cu", "bc1_noalloc.cu")]
     units += [(os.path.join(CSRC, "bc1_level.cu"), ["-DICBC_LEVEL=%d" % lv], "bc1_level%d.o" % lv)
               for lv in range(9, -1, -1)]
     units += [(os.path.join(CSRC, n), [], n.replace(".cu", ".o"))

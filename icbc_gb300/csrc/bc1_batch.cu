@@ -1,10 +1,27 @@
 // bc1_batch.cu -- persistent batched encoder over mixed images, levels and
-// decoders.  -fmad=false as for every encoder translation unit.
+// decoders.  -fmad=false as for every encoder translation unit.  Compiled
+// twice: -DICBC_BATCH_BYTES=1 keeps texels as bytes (batches without weight
+// planes: four CTAs per SM, as the plain image kernels), =0 as floats.
 #include <cuda_runtime.h>
 
 #include "bc1_loaders.cuh"
 
+#ifndef ICBC_BATCH_BYTES
+#error "compile with -DICBC_BATCH_BYTES=<0|1>"
+#endif
+
 namespace icbc_gpu {
+
+constexpr bool kBytes = ICBC_BATCH_BYTES != 0;
+
+// Encodes the warp's task at level L on its texel rows.
+template <int L, bool DEFER>
+__device__ __forceinline__ float encode_task(const WarpCtx &w, const ImageDesc &d, const EncodeParams &p, bool active,
+                                             uint32_t &c0, uint32_t &c1, uint32_t &idx, bool &pending) {
+    if (kBytes) return encode_warp_ex<L, DEFER>(w, byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA), p, active,
+                                                c0, c1, idx, pending);
+    return encode_warp_ex<L, DEFER>(w, float_row(w), p, active, c0, c1, idx, pending);
+}
 
 // Persistent batched encoder: every warp takes the next task (32 blocks of
 // one image) from an atomic counter until the queue is empty.  Tasks are
@@ -15,10 +32,10 @@ namespace icbc_gpu {
 // level-9 images leave refinement to k_refine's batch mode (bc1_refine.cu),
 // which runs after this kernel in the same stream: the same split as the
 // plain level-9 launches, so lanes do not wait for each other's refinement.
-__global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const GlobalTables *G, const ImageDesc *images,
-                                                                     const BatchTask *tasks, const uint32_t *task_start,
-                                                                     int n_images, int ntasks, int *counter,
-                                                                     const int64_t *refine_base, RefineSlot *slots) {
+template <bool BYTES>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, BYTES ? 4 : 1)
+    k_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, const uint32_t *task_start,
+                   int n_images, int ntasks, int *counter, const int64_t *refine_base, RefineSlot *slots) {
     extern __shared__ __align__(16) unsigned char smem[];
     SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
     stage_tables(T, G);
@@ -50,9 +67,12 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
         p.three_color_mode = d.three_color_mode;
         p.three_color_black = d.three_color_black;
         p.cw = v3(d.cw[0], d.cw[1], d.cw[2]);
-        const WarpCtx w = warp_ctx<9>(smem, T, G, p.decoder);
+        const WarpCtx w = BYTES ? warp_ctx_byte_rows(smem, T, G, p.decoder) : warp_ctx<9>(smem, T, G, p.decoder);
         __syncwarp();
-        if (active) load_image_block(d, b, w.in + lane * kInStride, T.lut255);
+        if (active) {
+            if (BYTES) load_image_block_bytes(d, b, reinterpret_cast<uint32_t *>(w.in) + lane * kInWordsByte);
+            else load_image_block(d, b, w.in + lane * kInStride, T.lut255);
+        }
         __syncwarp();
         uint32_t c0 = 0, c1 = 0, idx = 0;
         if (level >= 4 && active) {
@@ -67,18 +87,18 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
         bool pending = false;
         float e = 0.0f;
         switch (level) {
-            case 0: e = encode_warp<0>(w, p, active, c0, c1, idx); break;
-            case 1: e = encode_warp<1>(w, p, active, c0, c1, idx); break;
-            case 2: e = encode_warp<2>(w, p, active, c0, c1, idx); break;
-            case 3: e = encode_warp<3>(w, p, active, c0, c1, idx); break;
-            case 4: e = encode_warp<4>(w, p, active, c0, c1, idx); break;
-            case 5: e = encode_warp<5>(w, p, active, c0, c1, idx); break;
-            case 6: e = encode_warp<6>(w, p, active, c0, c1, idx); break;
-            case 7: e = encode_warp<7>(w, p, active, c0, c1, idx); break;
-            case 8: e = encode_warp<8>(w, p, active, c0, c1, idx); break;
+            case 0: e = encode_task<0, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 1: e = encode_task<1, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 2: e = encode_task<2, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 3: e = encode_task<3, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 4: e = encode_task<4, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 5: e = encode_task<5, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 6: e = encode_task<6, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 7: e = encode_task<7, false>(w, d, p, active, c0, c1, idx, pending); break;
+            case 8: e = encode_task<8, false>(w, d, p, active, c0, c1, idx, pending); break;
             default:
-                if (base >= 0) e = encode_warp_ex<9, true>(w, float_row(w), p, active, c0, c1, idx, pending);
-                else e = encode_warp<9>(w, p, active, c0, c1, idx);
+                if (base >= 0) e = encode_task<9, true>(w, d, p, active, c0, c1, idx, pending);
+                else e = encode_task<9, false>(w, d, p, active, c0, c1, idx, pending);
                 break;
         }
         if (active) {
@@ -89,22 +109,34 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_encode_batch(const Global
     }
 }
 
-cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
-                                const uint32_t *task_start, int n_images, int ntasks, int *counter,
-                                cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots) {
-    const size_t smem = smem_bytes(true);
-    cudaError_t e = cudaFuncSetAttribute(k_encode_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+#define ICBC_BATCH_CAT2(a, b) a##b
+#define ICBC_BATCH_CAT(a, b) ICBC_BATCH_CAT2(a, b)
+#if ICBC_BATCH_BYTES
+#define ICBC_BATCH_FN(name) ICBC_BATCH_CAT(name, _bytes)
+#else
+#define ICBC_BATCH_FN(name) ICBC_BATCH_CAT(name, _float)
+#endif
+
+static size_t batch_smem() { return kBytes ? smem_bytes_byte_rows() : smem_bytes(true); }
+
+cudaError_t ICBC_BATCH_FN(launch_encode_batch)(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                               const uint32_t *task_start, int n_images, int ntasks, int *counter,
+                                               cudaStream_t stream, int grid, const int64_t *refine_base,
+                                               RefineSlot *slots) {
+    const size_t smem = batch_smem();
+    cudaError_t e = cudaFuncSetAttribute(k_encode_batch<kBytes>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_encode_batch<<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, task_start, n_images, ntasks, counter,
-                                                               refine_base, slots);
+    k_encode_batch<kBytes><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, task_start, n_images, ntasks,
+                                                                       counter, refine_base, slots);
     return cudaGetLastError();
 }
 
-int batch_ctas_per_sm() {
+int ICBC_BATCH_FN(batch_ctas_per_sm)() {
     int n = 0;
-    const size_t smem = smem_bytes(true);
-    cudaFuncSetAttribute(k_encode_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_encode_batch, kWarpsPerCta * 32, smem) != cudaSuccess)
+    const size_t smem = batch_smem();
+    cudaFuncSetAttribute(k_encode_batch<kBytes>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_encode_batch<kBytes>, kWarpsPerCta * 32, smem) !=
+        cudaSuccess)
         return 1;
     return n > 0 ? n : 1;
 }

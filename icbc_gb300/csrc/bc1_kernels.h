@@ -65,11 +65,28 @@ ICBC_DECLARE_LEVEL(9)
 // With refine_base (one entry per image; -1: refine inline) a level-9 image's
 // refinement is deferred: block b's RefineSlot goes to slots[refine_base[i] + b]
 // and launch_refine_batch finishes it.  NULL refine_base: all inline.
-cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
-                                const uint32_t *task_start, int n_images, int ntasks, int *counter,
-                                cudaStream_t stream, int grid, const int64_t *refine_base = nullptr,
-                                RefineSlot *slots = nullptr);
-int batch_ctas_per_sm();
+// byte_rows: the kernel with byte texel rows (no image of the batch has a
+// weight plane), four CTAs per SM; else float rows.
+cudaError_t launch_encode_batch_float(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                      const uint32_t *task_start, int n_images, int ntasks, int *counter,
+                                      cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots);
+cudaError_t launch_encode_batch_bytes(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                      const uint32_t *task_start, int n_images, int ntasks, int *counter,
+                                      cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots);
+int batch_ctas_per_sm_float();
+int batch_ctas_per_sm_bytes();
+inline cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                       const uint32_t *task_start, int n_images, int ntasks, int *counter,
+                                       cudaStream_t stream, int grid, const int64_t *refine_base = nullptr,
+                                       RefineSlot *slots = nullptr, bool byte_rows = false) {
+    return byte_rows ? launch_encode_batch_bytes(G, images, tasks, task_start, n_images, ntasks, counter, stream, grid,
+                                                 refine_base, slots)
+                     : launch_encode_batch_float(G, images, tasks, task_start, n_images, ntasks, counter, stream, grid,
+                                                 refine_base, slots);
+}
+inline int batch_ctas_per_sm(bool byte_rows = false) {
+    return byte_rows ? batch_ctas_per_sm_bytes() : batch_ctas_per_sm_float();
+}
 cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder, cudaStream_t stream);
 cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
                             cudaStream_t stream);

@@ -517,7 +517,10 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     }
     icbc_gpu_batch *B = new icbc_gpu_batch();
     B->ntasks = (int)tasks.size();
-    B->grid = sm_count() * batch_ctas_per_sm();
+    // Byte texel rows (four CTAs per SM) unless an image brings a weight plane.
+    bool byte_rows = true;
+    for (int i = 0; i < n_images; i++) byte_rows &= descs[i].weight_mode != ICBC_GPU_WEIGHTS_PLANE;
+    B->grid = sm_count() * batch_ctas_per_sm(byte_rows);
     B->refine_total = refine_total;
     B->map_n = (int)map_image.size();
     cudaError_t e = cudaMalloc(&B->d_images, sizeof(ImageDesc) * std::max(1, n_images));
@@ -554,7 +557,7 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
         cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int), cs);
         cudaError_t e2 = e1 == cudaSuccess && B->ntasks
                              ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter,
-                                                   cs, B->grid, B->d_refine_base, B->d_slots)
+                                                   cs, B->grid, B->d_refine_base, B->d_slots, byte_rows)
                              : e1;
         if (e2 == cudaSuccess && refine_total) {
             e2 = cudaMemsetAsync(B->d_refine_counter, 0, sizeof(unsigned long long), cs);

@@ -205,8 +205,10 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
         // A persistent grid no larger than the batch's work (four tasks per
         // CTA at least), so small batches share the GPU instead of each
         // filling it.
+        // Requests carry uniform or alpha weights: the byte-row kernel.
         e = launch_encode_batch(S->G, slot.d_images, nullptr, slot.d_start, n, (int)total, slot.d_counter,
-                                slot.stream, (int)std::min<uint32_t>((uint32_t)S->grid, (total + 3) / 4));
+                                slot.stream, (int)std::min<uint32_t>((uint32_t)S->grid, (total + 3) / 4), nullptr,
+                                nullptr, true);
     for (size_t i = 0; i < reqs.size() && e == cudaSuccess; i++) {
         Request *q = reqs[i];
         const ImageDesc &d = slot.h_images[i];
@@ -328,7 +330,7 @@ int icbc_gpu_server_create(const icbc_gpu_server_config *config, icbc_gpu_server
     cudaGetDevice(&S->device);
     int per_sm = 1;
     cudaDeviceGetAttribute(&S->grid, cudaDevAttrMultiProcessorCount, S->device);
-    per_sm = batch_ctas_per_sm();
+    per_sm = batch_ctas_per_sm(true);
     S->grid *= per_sm;
     const size_t budget = round_up((size_t)config->hbm_budget_bytes, kGranule);
     // Pinned staging for blocks and errors (an eighth and a sixteenth of the
