@@ -59,11 +59,11 @@ REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
 
 # DRAM bytes per level call (dram__bytes_read.sum + dram__bytes_write.sum of
 # its launches) from one ncu capture of this workload, summarised in
-# profiles/k_encode_image_L8_L9_k_refine_quality_sweep_4096.md.  Level 9 is
-# the encoder plus the refinement pass; each reads the 64 MB image.
-NCU_TRAFFIC_BYTES = {8: 75.61e6 + 0.85e6, 9: (75.68e6 + 2.82e6) + (76.00e6 + 2.16e6)}
+# profiles/k_encode_image_bytes_L8_L9_k_refine_quality_sweep_4096.md.  Level 9
+# is the encoder plus the refinement pass; each reads the 64 MB image.
+NCU_TRAFFIC_BYTES = {8: 75.66e6 + 1.59e6, 9: (75.64e6 + 3.35e6) + (75.96e6 + 2.18e6)}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum per level call, " \
-                 "profiles/k_encode_image_L8_L9_k_refine_quality_sweep_4096.md"
+                 "profiles/k_encode_image_bytes_L8_L9_k_refine_quality_sweep_4096.md"
 
 
 def algorithmic_ops(stats: dict, level: int) -> float:
