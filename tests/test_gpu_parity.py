@@ -259,6 +259,26 @@ def test_host_buffer_path_in_bands(gpu_lib):
             assert np.array_equal(out, ob) and same_bits(errs, oe)
 
 
+def test_byte_rows_equal_float_rows(gpu_lib):
+    """The RGBA8 kernels keep texels as bytes (alpha weights read through the
+    i/255 table); a weight plane holding the same alpha/255 floats takes the
+    float-row kernels.  Same floats in, so the same bytes and errors out."""
+    import torch
+    ig = gpu_lib
+    img = synth.quality_sweep_image(260, 140, seed=31)
+    dev = _to_dev(img)
+    plane = torch.from_numpy((img[..., 3].astype(np.float64) / 255.0).astype(np.float32)).cuda()
+    lut = (np.arange(256, dtype=np.float32) / np.float32(255.0)).astype(np.float32)
+    assert np.array_equal(plane.cpu().numpy(), lut[img[..., 3]])
+    for level in range(2, 10):
+        for dec in (0, 3):
+            ob, oe = ig.compress_image(dev, level, dec, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA, with_errors=True)
+            fb, fe = ig.compress_image(dev, level, dec, (0.299, 0.587, 0.114), ig.WEIGHTS_PLANE, plane,
+                                       with_errors=True)
+            assert torch.equal(ob, fb), (level, dec)
+            assert same_bits(oe.cpu().numpy(), fe.cpu().numpy()), (level, dec)
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib
