@@ -361,7 +361,8 @@ def run_ours(args):
         "batch": batch,
         "serving": serving,
         "hard": hard,
-        "gpu_launches": args.steps * len(LEVELS),
+        # one encoder launch per level and step; level 9 adds its refinement pass
+        "gpu_launches": args.steps * (len(LEVELS) + (1 if 9 in LEVELS else 0)),
         "clocks": clk,
         "wall_s_timed": wall,
     }
