@@ -718,10 +718,11 @@ int icbc_gpu_compress_bc1_image_host(const uint8_t *rgba, int32_t width, int32_t
     if (e != cudaSuccess) return set_cuda_error(e);
     // Bands of at least 64 block rows (whole block rows, so each band is an
     // independent image whose last band alone meets the bottom edge).  Level
-    // 9 stays one band: its refinement queue needs many blocks per lane to
-    // balance (banded, it was 8% slower end to end; every other level was
-    // 5-40% faster).
-    const int bands = level == 9 ? 1 : (int)std::max<int64_t>(1, std::min<int64_t>(kMaxBands, bh / 64));
+    // 9 takes at most two bands of 256+ block rows: its refinement queue
+    // needs many blocks per lane to balance (in eight bands it was 8% slower
+    // end to end, in two 3% faster; every other level gains 5-40% from eight).
+    const int bands = level == 9 ? (int)std::max<int64_t>(1, std::min<int64_t>(2, bh / 256))
+                                 : (int)std::max<int64_t>(1, std::min<int64_t>(kMaxBands, bh / 64));
     const int64_t rows_per = (bh + bands - 1) / bands;
     int st = ICBC_GPU_OK;
     for (int i = 0; i < bands && st == ICBC_GPU_OK; i++) {

@@ -240,7 +240,7 @@ def test_host_buffer_path_in_bands(gpu_lib):
     path and the oracle, weight planes and level 4+ prior output included."""
     import torch
     ig = gpu_lib
-    w, h = 1030, 602  # 151 block rows: 2 bands, the last one with a partial block row
+    w, h = 1030, 2050  # 513 block rows: 8 bands (2 at level 9), the last one with a partial block row
     img = synth.quality_sweep_image(w, h, seed=21)
     plane = np.random.default_rng(3).random((h, w), dtype=np.float32)
     dev = _to_dev(img)
