@@ -741,10 +741,16 @@ __device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g,
 // into the next block with work when this one is done.  `next` is the table
 // entry of the following combination, loaded one iteration ahead; a block
 // change reloads it.
+// One step, in two parts: walker_fold folds the error of combination k in
+// and moves to k + 1; walker_cross, when the walker has left its block with
+// work still to do, flushes it and enters the next block with work (`next`,
+// the table entry loaded one iteration ahead, is reloaded).  The search
+// checks for crossings once per iteration for the whole warp, so the rare
+// divergent crossing code stays off the common path.
 // With SIMD the walker keeps the smallest (error, simd_rank) of its share
 // in best / best_k (best_k holds the rank), never an error of FLT_MAX.
-template <bool FOUR, bool SIMD = false>
-__device__ __forceinline__ void walker_step(const WarpCtx &w, Walker &v, float e, uint32_t &next, int vec = 1) {
+template <bool SIMD = false>
+__device__ __forceinline__ void walker_fold(Walker &v, float e, int vec = 1) {
     const bool live = v.g < v.gend;
     bool better;
     int rk = v.k;
@@ -758,13 +764,17 @@ __device__ __forceinline__ void walker_step(const WarpCtx &w, Walker &v, float e
     v.best_k = better ? rk : v.best_k;
     v.g += live;
     v.k += live;
-    if (live && v.k == v.total && v.g < v.gend) {
-        walker_flush(w, v);
-        int nb = v.b + 1;
-        while ((block_info(w, nb) >> 16) == 0) nb++;
-        walker_enter<FOUR, SIMD>(w, v, nb, 0, vec);
-        next = (FOUR ? w.T->four : w.T->three)[0];
-    }
+}
+
+__device__ __forceinline__ bool walker_crossing(const Walker &v) { return v.k == v.total && v.g < v.gend; }
+
+template <bool FOUR, bool SIMD = false>
+__device__ __forceinline__ void walker_cross(const WarpCtx &w, Walker &v, uint32_t &next, int vec = 1) {
+    walker_flush(w, v);
+    int nb = v.b + 1;
+    while ((block_info(w, nb) >> 16) == 0) nb++;
+    walker_enter<FOUR, SIMD>(w, v, nb, 0, vec);
+    next = (FOUR ? w.T->four : w.T->three)[0];
 }
 
 // Returns this lane's winning table index, or -1 (no search, or no error
@@ -810,8 +820,13 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
             ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
             eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
         }
-        walker_step<FOUR, SIMD>(w, A, ea, na, vec);
-        walker_step<FOUR, SIMD>(w, B, eb, nb, vec);
+        walker_fold<SIMD>(A, ea, vec);
+        walker_fold<SIMD>(B, eb, vec);
+        const bool xa = walker_crossing(A), xb = walker_crossing(B);
+        if (__any_sync(kFull, xa || xb)) {
+            if (xa) walker_cross<FOUR, SIMD>(w, A, na, vec);
+            if (xb) walker_cross<FOUR, SIMD>(w, B, nb, vec);
+        }
         pa = na;
         pb = nb;
     }
