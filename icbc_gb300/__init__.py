@@ -170,6 +170,13 @@ def _torch():
     return torch
 
 
+def _on(stream):
+    """Stream context for the staging a call does before its launch (copies,
+    zeroed outputs), so it is ordered before the launch on `stream`."""
+    import contextlib
+    return _torch().cuda.stream(stream) if stream is not None else contextlib.nullcontext()
+
+
 def _stream_ptr(stream=None):
     torch = _torch()
     s = stream if stream is not None else torch.cuda.current_stream()
@@ -254,6 +261,13 @@ def compress_blocks(colors, weights, level: int, decoder: int = DECODER_DEFAULT,
     """
     torch = _torch()
     L = load()
+    with _on(stream):
+        return _compress_blocks(torch, L, colors, weights, level, decoder, color_weights, three_color_mode,
+                                three_color_black, initial, stream, out, errors, simd_profile)
+
+
+def _compress_blocks(torch, L, colors, weights, level, decoder, color_weights, three_color_mode, three_color_black,
+                     initial, stream, out, errors, simd_profile):
     on_host = not (hasattr(colors, "is_cuda") and colors.is_cuda)
     dev = torch.device("cuda")
     c = torch.as_tensor(np.ascontiguousarray(colors, np.float32) if on_host else colors).to(dev)
@@ -320,10 +334,11 @@ def compress_image(rgba, level: int, decoder: int = DECODER_DEFAULT, color_weigh
     L = load()
     h, w = int(rgba.shape[0]), int(rgba.shape[1])
     nb = blocks_of(w, h)
-    if out is None:
-        out = torch.zeros((nb, 8), dtype=torch.uint8, device=rgba.device)
-    if errors is None and with_errors:
-        errors = torch.empty(nb, dtype=torch.float32, device=rgba.device)
+    with _on(stream):  # the zeroed output is ordered before the launch
+        if out is None:
+            out = torch.zeros((nb, 8), dtype=torch.uint8, device=rgba.device)
+        if errors is None and with_errors:
+            errors = torch.empty(nb, dtype=torch.float32, device=rgba.device)
     d = image_desc(rgba, level, out, errors, decoder, color_weights, weight_mode, weight_plane, three_color_mode,
                    three_color_black)
     if simd_profile:
@@ -370,9 +385,11 @@ def decode_blocks(blocks, decoder: int = Decoder_D3D10, stream=None):
     """decode_bc1 over a CUDA uint8 tensor (n,8) -> (n,64) RGBA8."""
     torch = _torch()
     n = blocks.shape[0]
-    out = torch.empty((n, 64), dtype=torch.uint8, device=blocks.device)
-    _check(load().icbc_gpu_decode_bc1(blocks.contiguous().data_ptr(), out.data_ptr(), n, int(decoder),
-                                      _stream_ptr(stream)), "decode_bc1")
+    with _on(stream):  # a contiguous copy, if any, is ordered before the launch
+        b = blocks.contiguous()
+        out = torch.empty((n, 64), dtype=torch.uint8, device=blocks.device)
+        _check(load().icbc_gpu_decode_bc1(b.data_ptr(), out.data_ptr(), n, int(decoder), _stream_ptr(stream)),
+               "decode_bc1")
     return out
 
 
@@ -380,10 +397,11 @@ def evaluate_errors(rgba_blocks, blocks, decoder: int = Decoder_D3D10, stream=No
     """evaluate_bc1_error over CUDA tensors (n,64) uint8 and (n,8) uint8 -> (n,) float32."""
     torch = _torch()
     n = blocks.shape[0]
-    out = torch.empty(n, dtype=torch.float32, device=blocks.device)
-    _check(load().icbc_gpu_evaluate_bc1_error(rgba_blocks.contiguous().data_ptr(), blocks.contiguous().data_ptr(),
-                                              out.data_ptr(), n, int(decoder), _stream_ptr(stream)),
-           "evaluate_bc1_error")
+    with _on(stream):  # contiguous copies, if any, are ordered before the launch
+        r, b = rgba_blocks.contiguous(), blocks.contiguous()
+        out = torch.empty(n, dtype=torch.float32, device=blocks.device)
+        _check(load().icbc_gpu_evaluate_bc1_error(r.data_ptr(), b.data_ptr(), out.data_ptr(), n, int(decoder),
+                                                  _stream_ptr(stream)), "evaluate_bc1_error")
     return out
 
 
@@ -483,8 +501,9 @@ def compress_mips(rgba, level: int, levels: int | None = None, decoder: int = DE
     torch = _torch()
     h, w = int(rgba.shape[0]), int(rgba.shape[1])
     ws, hs, off = mip_layout(w, h, levels)
-    out = torch.zeros((off[-1], 8), dtype=torch.uint8, device=rgba.device)
-    errors = torch.empty(off[-1], dtype=torch.float32, device=rgba.device) if with_errors else None
+    with _on(stream):  # the zeroed output is ordered before the launches
+        out = torch.zeros((off[-1], 8), dtype=torch.uint8, device=rgba.device)
+        errors = torch.empty(off[-1], dtype=torch.float32, device=rgba.device) if with_errors else None
     d = image_desc(rgba, level, out, errors, decoder, color_weights, weight_mode, None, three_color_mode,
                    three_color_black)
     _check(load().icbc_gpu_compress_bc1_mips(ctypes.byref(d), len(ws), _stream_ptr(stream)), "compress_bc1_mips")
@@ -597,8 +616,10 @@ def autotune(image, levels=range(10), candidates=TUNE_CANDIDATES, repeats: int =
     import json
     torch = _torch()
     nb = blocks_of(int(image.shape[1]), int(image.shape[0]))
-    out = torch.zeros((nb, 8), dtype=torch.uint8, device=image.device)
     stream = torch.cuda.Stream(device=image.device)
+    stream.wait_stream(torch.cuda.current_stream())  # the image is ready
+    with torch.cuda.stream(stream):
+        out = torch.zeros((nb, 8), dtype=torch.uint8, device=image.device)
     table = {}
     for lv in levels:
         before = get_launch_config(lv)

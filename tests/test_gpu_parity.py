@@ -279,6 +279,54 @@ def test_byte_rows_equal_float_rows(gpu_lib):
             assert same_bits(oe.cpu().numpy(), fe.cpu().numpy()), (level, dec)
 
 
+def test_concurrent_calls_on_own_streams(gpu_lib):
+    """Calls are thread-safe per stream: four host threads encode different
+    images (levels 3, 8 and 9, image, float-block and host-buffer forms) on
+    their own streams at once; every result equals the same call made alone."""
+    import threading
+    import torch
+    ig = gpu_lib
+    jobs = []
+    for i in range(4):
+        img = synth.quality_sweep_image(300 + 40 * i, 200 + 24 * i, seed=70 + i)
+        jobs.append((img, _to_dev(img), (3, 8, 9, 9)[i], i % 4))
+    alone = []
+    for img, dev, level, dec in jobs:
+        a = ig.compress_image(dev, level, dec, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA).cpu().numpy()
+        cols, w, _ = O.image_blocks(img, weight_mode=1)
+        b, _ = ig.compress_blocks(cols, w, level, dec, (0.299, 0.587, 0.114))
+        c = ig.compress_image_host(img, level, dec, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA)
+        alone.append((a, b, c, cols, w))
+    results = [None] * 4
+    errors = []
+
+    def work(k):
+        try:
+            img, dev, level, dec = jobs[k]
+            s = torch.cuda.Stream()
+            got = []
+            for _ in range(3):
+                with torch.cuda.stream(s):
+                    out = ig.compress_image(dev, level, dec, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA, stream=s)
+                s.synchronize()
+                b, _ = ig.compress_blocks(alone[k][3], alone[k][4], level, dec, (0.299, 0.587, 0.114), stream=s)
+                c = ig.compress_image_host(img, level, dec, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA)
+                got.append((out.cpu().numpy(), b, c))
+            results[k] = got
+        except Exception as e:  # surfaced below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for k in range(4):
+        for a, b, c in results[k]:
+            assert np.array_equal(a, alone[k][0]) and np.array_equal(b, alone[k][1]) and np.array_equal(c, alone[k][2]), k
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib
