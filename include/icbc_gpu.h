@@ -273,8 +273,9 @@ int icbc_gpu_server_destroy(icbc_gpu_server *server);
 /* ------------------------------------------------------------------------
  * Containers for encoded images (icbc_test.cpp:155-279).  `blocks` are
  * ceil(w/4) * ceil(h/4) BC1 blocks in row-major block order, in host or
- * device memory (device blocks are copied out first).  Headers hold the
- * image's own width and height; the data size is 8 bytes per block.
+ * device memory (device blocks are copied out first, after the caller has
+ * synchronised the stream that wrote them).  Headers hold the image's own
+ * width and height; the data size is 8 bytes per block.
  * ---------------------------------------------------------------------- */
 /* DDS with a DXT1 FourCC and one mip level (icbc_test.cpp:155-211). */
 int icbc_gpu_write_dds(const char *path, int32_t width, int32_t height, const void *blocks);
