@@ -120,7 +120,94 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_encode_image_bytes(con
     }
 }
 
+// Levels 2..5 in two passes (RGBA8 images, byte rows).  At these thresholds
+// most blocks reduce to 0 or 1 colours (on the quality-sweep image 99% at
+// level 2, 86% at level 4, 61% at level 5), and a warp with one other block
+// among them runs that block's whole cluster fit with one lane busy.  Pass 1
+// reduces every block, finishes those of 0 or 1 colours and lists the rest;
+// pass 2 runs the full encoder over the list, 32 listed blocks per warp.
+// Each block's computation is the single-pass one (pass 2 reduces again).
+// Levels 2-5 take 49-61% less time this way; at level 6 (29% trivial blocks)
+// the second reduction costs more than it saves.
+template <int L>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_trivial(const GlobalTables *G, ImageDesc d,
+                                                                        EncodeParams p, uint32_t *list,
+                                                                        unsigned int *listed) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    const WarpCtx w = warp_ctx_byte_rows(smem, T, G, p.decoder);
+    const ByteRow row = byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA);
+    float *srow = w.sat + w.lane * kSatStride;
+    const int64_t groups = (d.nblocks + 31) / 32;
+    for (int64_t g = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); g < groups;
+         g += (int64_t)gridDim.x * kWarpsPerCta) {
+        const int64_t b = g * 32 + w.lane;
+        const bool active = b < d.nblocks;
+        __syncwarp();
+        if (active) load_image_block_bytes(d, b, reinterpret_cast<uint32_t *>(w.in) + w.lane * kInWordsByte);
+        __syncwarp();
+        bool other = false;
+        if (active) {
+            bool any_black;
+            const int count = reduce_colors(row, Level<L>::threshold, srow, any_black);
+            if (count <= 1) {
+                uint32_t c0, c1, idx;
+                const float e = trivial_block(w, row, p, srow, count, c0, c1, idx);
+                d.out[b] = make_uint2(c0 | (c1 << 16), idx);
+                if (d.errors) d.errors[b] = e;
+            } else {
+                other = true;
+            }
+        }
+        const unsigned m = __ballot_sync(kFull, other);
+        if (m) {
+            unsigned base = 0;
+            if (w.lane == 0) base = atomicAdd(listed, (unsigned)__popc(m));
+            base = __shfl_sync(kFull, base, 0);
+            if (other) list[base + __popc(m & ((1u << w.lane) - 1u))] = (uint32_t)b;
+        }
+    }
+}
+
+template <int L>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_listed(const GlobalTables *G, ImageDesc d,
+                                                                       EncodeParams p, const uint32_t *list,
+                                                                       const unsigned int *listed) {
+    const int64_t n = *listed;
+    const int64_t groups = (n + 31) / 32;
+    if ((int64_t)blockIdx.x * kWarpsPerCta >= groups) return;  // the whole CTA has no work
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    const WarpCtx w = warp_ctx_byte_rows(smem, T, G, p.decoder);
+    const ByteRow row = byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA);
+    for (int64_t g = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); g < groups;
+         g += (int64_t)gridDim.x * kWarpsPerCta) {
+        const int64_t k = g * 32 + w.lane;
+        const bool active = k < n;
+        const int64_t b = active ? (int64_t)list[k] : 0;
+        __syncwarp();
+        if (active) load_image_block_bytes(d, b, reinterpret_cast<uint32_t *>(w.in) + w.lane * kInWordsByte);
+        __syncwarp();
+        uint32_t c0 = 0, c1 = 0, idx = 0;
+        if (L >= 4 && active) {
+            const uint2 prev = d.out[b];
+            c0 = prev.x & 0xffff;
+            c1 = prev.x >> 16;
+            idx = prev.y;
+        }
+        bool pending;
+        const float e = encode_warp_ex<L, false>(w, row, p, active, c0, c1, idx, pending);
+        if (active) {
+            d.out[b] = make_uint2(c0 | (c1 << 16), idx);
+            if (d.errors) d.errors[b] = e;
+        }
+    }
+}
+
 constexpr int L = ICBC_LEVEL;
+constexpr bool kCompact = L >= 2 && L <= 5;
 
 // CTAs for n blocks, from the level's launch shape: every warp takes
 // groups_per_warp groups of 32 blocks; a persistent grid is exactly the
@@ -200,8 +287,50 @@ static int g_resident_blocks = 0, g_resident_image = 0, g_resident_bytes = 0;
 // alpha); weight planes need float rows.
 static bool use_byte_rows(const ImageDesc &d) { return Level<L>::cluster && d.weight_mode != ICBC_GPU_WEIGHTS_PLANE; }
 
+static int g_resident_trivial = 0, g_resident_listed = 0;
+
+// The two passes of kCompact levels, with the list in stream-ordered scratch.
+static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
+                                          cudaStream_t stream, int sms) {
+    const size_t smem = smem_bytes_byte_rows();
+    cudaError_t e = cudaFuncSetAttribute(k_image_trivial<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_image_listed<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && !g_resident_listed) {
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_image_listed<L>, kWarpsPerCta * 32, smem);
+        g_resident_listed = per_sm > 0 ? per_sm : 1;
+    }
+    if (e != cudaSuccess) return e;
+    const size_t list_bytes = ((size_t)d.nblocks * 4 + 15) / 16 * 16;
+    void *scratch = nullptr;
+    e = scratch_alloc(&scratch, list_bytes + 16, stream);
+    if (e != cudaSuccess) return e;
+    uint32_t *list = static_cast<uint32_t *>(scratch);
+    unsigned int *listed = reinterpret_cast<unsigned int *>(static_cast<char *>(scratch) + list_bytes);
+    e = cudaMemsetAsync(listed, 0, sizeof(unsigned int), stream);
+    if (e == cudaSuccess) {
+        const int grid = grid_for(k_image_trivial<L>, d.nblocks, sms, smem, g_resident_trivial);
+        k_image_trivial<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        // Persistent over the list, whose length only the device knows.
+        const int64_t most = ((int64_t)d.nblocks + 32 * kWarpsPerCta - 1) / (32 * kWarpsPerCta);
+        const int64_t cap = (int64_t)sms * g_resident_listed;
+        const int grid = (int)(most < cap ? most : cap);
+        k_image_listed<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed);
+        e = cudaGetLastError();
+    }
+    const cudaError_t f = scratch_free(scratch, stream);
+    return e != cudaSuccess ? e : f;
+}
+
 static cudaError_t launch_image(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p, cudaStream_t stream,
                                 int sms, RefineSlot *ext_st, unsigned long long *ext_counter) {
+    if constexpr (kCompact) {
+        if (use_byte_rows(d) && d.nblocks < (int64_t(1) << 32)) return launch_image_compacted(G, d, p, stream, sms);
+    }
     if constexpr (Level<L>::cluster) {
         if (use_byte_rows(d))
             return run(k_encode_image_bytes<L, kDefer>, smem_bytes_byte_rows(), g_resident_bytes, d.nblocks, sms,
