@@ -66,6 +66,13 @@ TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum per level cal
                  "profiles/k_encode_image_bytes_L8_L9_k_refine_quality_sweep_4096.md"
 
 
+def launches_per_level(level: int) -> int:
+    """Kernel launches of one level call on the RGBA8 image: levels 2-5 run in
+    two passes (trivial blocks, then the listed rest), level 9 adds its
+    refinement pass."""
+    return 2 if 2 <= level <= 5 or level == 9 else 1
+
+
 def level_kernels(level: int) -> str:
     """The launches of one level call on the RGBA8 image with alpha weights."""
     if level < 2:
@@ -368,8 +375,7 @@ def run_ours(args):
         "batch": batch,
         "serving": serving,
         "hard": hard,
-        # one encoder launch per level and step; level 9 adds its refinement pass
-        "gpu_launches": args.steps * (len(LEVELS) + (1 if 9 in LEVELS else 0)),
+        "gpu_launches": args.steps * sum(launches_per_level(lv) for lv in LEVELS),
         "clocks": clk,
         "wall_s_timed": wall,
     }
