@@ -327,6 +327,24 @@ def test_concurrent_calls_on_own_streams(gpu_lib):
             assert np.array_equal(a, alone[k][0]) and np.array_equal(b, alone[k][1]) and np.array_equal(c, alone[k][2]), k
 
 
+def test_two_pass_levels_edge_cases(gpu_lib):
+    """Levels 2-5 list the blocks of two or more reduced colours in a first
+    pass: an image with none (flat), one with all (noise) and a mixed one with
+    partial edge blocks all equal the oracle, blocks and errors."""
+    ig = gpu_lib
+    rng = np.random.default_rng(17)
+    flat = np.full((36, 52, 4), 200, np.uint8)
+    noise = rng.integers(0, 256, (40, 44, 4), dtype=np.uint8)
+    mixed = synth.quality_sweep_image(101, 67, seed=5)
+    for img in (flat, noise, mixed):
+        dev = _to_dev(img)
+        for level in (2, 3, 4, 5):
+            out, err = ig.compress_image(dev, level, 1, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA, with_errors=True)
+            ob, oe = O.encode_image(img, level, 1, (0.299, 0.587, 0.114), 1, None, True, True, nthreads=8)
+            assert np.array_equal(out.cpu().numpy(), ob), (img.shape, level)
+            assert same_bits(err.cpu().numpy(), oe), (img.shape, level)
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib
