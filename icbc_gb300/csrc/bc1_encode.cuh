@@ -851,18 +851,17 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 __device__ __forceinline__ FloatRow float_row(const WarpCtx &w) { return FloatRow{w.in + w.lane * kInStride}; }
 
 // The blocks of 0 or 1 reduced colours (icbc.h:3752-3764): the zero block, or
-// the optimal single-colour endpoints with their error.  srow holds the
-// reduced colour.
-template <class Row>
-__device__ __forceinline__ float trivial_block(const WarpCtx &w, const Row &row, const EncodeParams &p,
-                                               const float *srow, int count, uint32_t &c0, uint32_t &c1,
-                                               uint32_t &idx) {
+// the optimal single-colour endpoints of `color` with their error.
+template <int UNROLL = 1, class Row>
+__device__ __forceinline__ float trivial_block(const DecoderTables *D, const float *lut255, const Row &row,
+                                               const EncodeParams &p, V3 color, int count, uint32_t &c0,
+                                               uint32_t &c1, uint32_t &idx) {
     if (count == 0) {
         c0 = c1 = idx = 0;
         return 0.0f;
     }
-    single_color(w.D, xyz(ld4(srow)), c0, c1, idx);
-    return block_error(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D), idx);
+    single_color(D, color, c0, c1, idx);
+    return block_error<UNROLL>(row, p.cw, palette_f(c0, c1, p.decoder, lut255, D), idx);
 }
 
 template <int L, bool DEFER, bool SIMD = false, class Row>
@@ -879,7 +878,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
     if (active) {
         if (O::cluster) count = reduce_colors(row, O::threshold, srow, any_black);
         if (O::cluster && count <= 1) {
-            err = trivial_block(w, row, p, srow, count, c0, c1, idx);
+            err = trivial_block(w.D, w.T->lut255, row, p, xyz(ld4(srow)), count, c0, c1, idx);
         } else {
             live = true;
             err = FLT_MAX;

@@ -129,43 +129,67 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_encode_image_bytes(con
 // Each block's computation is the single-pass one (pass 2 reduces again).
 // Levels 2-5 take 49-61% less time this way; at level 6 (29% trivial blocks)
 // the second reduction costs more than it saves.
+// Pass 1 needs only to tell blocks of 0 or 1 reduced colours from the rest,
+// so it follows reduce_colors (icbc.h:1683-1728) only while one colour has
+// been kept: the texels and the running colour stay in registers (a ByteRow
+// over a register array, every index known at compile time), and a block
+// is listed as soon as a second colour appears.  For the blocks it finishes
+// the arithmetic is reduce_colors' (every texel merged into the first
+// colour).  Shared memory holds only the i / 255 table; six CTAs per SM
+// (80 registers) beat both four (126 registers) and eight (more spills).
 template <int L>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_trivial(const GlobalTables *G, ImageDesc d,
-                                                                        EncodeParams p, uint32_t *list,
-                                                                        unsigned int *listed) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
-    stage_tables(T, G);
-    const WarpCtx w = warp_ctx_byte_rows(smem, T, G, p.decoder);
-    const ByteRow row = byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA);
-    float *srow = w.sat + w.lane * kSatStride;
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 6) k_image_trivial(const GlobalTables *G, ImageDesc d, EncodeParams p,
+                                                                     uint32_t *list, unsigned int *listed) {
+    __shared__ float lut[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = G->s.lut255[i];
+    __syncthreads();
+    const DecoderTables *D = &G->dec[p.decoder];
+    const int lane = threadIdx.x & 31;
+    const int alpha = d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA;
     const int64_t groups = (d.nblocks + 31) / 32;
     for (int64_t g = (int64_t)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); g < groups;
          g += (int64_t)gridDim.x * kWarpsPerCta) {
-        const int64_t b = g * 32 + w.lane;
+        const int64_t b = g * 32 + lane;
         const bool active = b < d.nblocks;
-        __syncwarp();
-        if (active) load_image_block_bytes(d, b, reinterpret_cast<uint32_t *>(w.in) + w.lane * kInWordsByte);
-        __syncwarp();
         bool other = false;
         if (active) {
-            bool any_black;
-            const int count = reduce_colors(row, Level<L>::threshold, srow, any_black);
-            if (count <= 1) {
+            uint32_t px[16];
+            fetch_image_block(d, b, px);
+            const ByteRow row{px, lut, alpha};
+            V3 c = v3(0.0f, 0.0f, 0.0f);
+            float wc = 0.0f;
+            int count = 0;
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                const V3 ct = row.color(t);
+                const float wt = row.weight(t);
+                if (!other && wt > 0) {
+                    if (count == 0) {
+                        c = ct;
+                        wc = wt;
+                        count = 1;
+                    } else if (near3(c, ct, Level<L>::threshold)) {
+                        const float s = wc + wt;
+                        c = v3((c.x * wc + ct.x * wt) / s, (c.y * wc + ct.y * wt) / s, (c.z * wc + ct.z * wt) / s);
+                        wc = s;
+                    } else {
+                        other = true;
+                    }
+                }
+            }
+            if (!other) {
                 uint32_t c0, c1, idx;
-                const float e = trivial_block(w, row, p, srow, count, c0, c1, idx);
+                const float e = trivial_block<16>(D, lut, row, p, c, count, c0, c1, idx);
                 d.out[b] = make_uint2(c0 | (c1 << 16), idx);
                 if (d.errors) d.errors[b] = e;
-            } else {
-                other = true;
             }
         }
         const unsigned m = __ballot_sync(kFull, other);
         if (m) {
             unsigned base = 0;
-            if (w.lane == 0) base = atomicAdd(listed, (unsigned)__popc(m));
+            if (lane == 0) base = atomicAdd(listed, (unsigned)__popc(m));
             base = __shfl_sync(kFull, base, 0);
-            if (other) list[base + __popc(m & ((1u << w.lane) - 1u))] = (uint32_t)b;
+            if (other) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)b;
         }
     }
 }
@@ -293,9 +317,7 @@ static int g_resident_trivial = 0, g_resident_listed = 0;
 static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
                                           cudaStream_t stream, int sms) {
     const size_t smem = smem_bytes_byte_rows();
-    cudaError_t e = cudaFuncSetAttribute(k_image_trivial<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_image_listed<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_image_listed<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && !g_resident_listed) {
         int per_sm = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_image_listed<L>, kWarpsPerCta * 32, smem);
@@ -310,8 +332,8 @@ static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc
     unsigned int *listed = reinterpret_cast<unsigned int *>(static_cast<char *>(scratch) + list_bytes);
     e = cudaMemsetAsync(listed, 0, sizeof(unsigned int), stream);
     if (e == cudaSuccess) {
-        const int grid = grid_for(k_image_trivial<L>, d.nblocks, sms, smem, g_resident_trivial);
-        k_image_trivial<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed);
+        const int grid = grid_for(k_image_trivial<L>, d.nblocks, sms, 0, g_resident_trivial);
+        k_image_trivial<L><<<grid, kWarpsPerCta * 32, 0, stream>>>(G, d, p, list, listed);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
