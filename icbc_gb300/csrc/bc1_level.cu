@@ -120,15 +120,15 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_encode_image_bytes(con
     }
 }
 
-// Levels 2..5 in two passes (RGBA8 images, byte rows).  At these thresholds
-// most blocks reduce to 0 or 1 colours (on the quality-sweep image 99% at
-// level 2, 86% at level 4, 61% at level 5), and a warp with one other block
-// among them runs that block's whole cluster fit with one lane busy.  Pass 1
-// reduces every block, finishes those of 0 or 1 colours and lists the rest;
-// pass 2 runs the full encoder over the list, 32 listed blocks per warp.
-// Each block's computation is the single-pass one (pass 2 reduces again).
-// Levels 2-5 take 49-61% less time this way; at level 6 (29% trivial blocks)
-// the second reduction costs more than it saves.
+// Levels 2..9 in two passes (RGBA8 images, byte rows).  Many blocks reduce
+// to 0 or 1 colours (on the quality-sweep image 99% at level 2, 86% at level
+// 4, 61% at level 5, 21-29% at levels 6-9), and a warp with one other block
+// among them runs that block's whole cluster fit with some lanes idle (with
+// one lane busy at the low levels).  Pass 1 finishes the blocks of 0 or 1
+// colours and lists the rest; pass 2 runs the full encoder over the list, 32
+// listed blocks per warp.  Each block's computation is the single-pass one
+// (pass 2 reduces again).  Levels 2-4 take half the time, levels 5-8 2-25%
+// less.
 // Pass 1 needs only to tell blocks of 0 or 1 reduced colours from the rest,
 // so it follows reduce_colors (icbc.h:1683-1728) only while one colour has
 // been kept: the texels and the running colour stay in registers (a ByteRow
@@ -139,7 +139,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_encode_image_bytes(con
 // (80 registers) beat both four (126 registers) and eight (more spills).
 template <int L>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 6) k_image_trivial(const GlobalTables *G, ImageDesc d, EncodeParams p,
-                                                                     uint32_t *list, unsigned int *listed) {
+                                                                     uint32_t *list, unsigned int *listed,
+                                                                     RefineSlot *st) {
     __shared__ float lut[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = G->s.lut255[i];
     __syncthreads();
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 6) k_image_trivial(const Gl
                 const float e = trivial_block<16>(D, lut, row, p, c, count, c0, c1, idx);
                 d.out[b] = make_uint2(c0 | (c1 << 16), idx);
                 if (d.errors) d.errors[b] = e;
+                if (st) st[b] = RefineSlot{e, 0u};  // level 9: nothing to refine
             }
         }
         const unsigned m = __ballot_sync(kFull, other);
@@ -194,10 +196,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 6) k_image_trivial(const Gl
     }
 }
 
-template <int L>
+template <int L, bool DEFER>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_listed(const GlobalTables *G, ImageDesc d,
                                                                        EncodeParams p, const uint32_t *list,
-                                                                       const unsigned int *listed) {
+                                                                       const unsigned int *listed, RefineSlot *st) {
     const int64_t n = *listed;
     const int64_t groups = (n + 31) / 32;
     if ((int64_t)blockIdx.x * kWarpsPerCta >= groups) return;  // the whole CTA has no work
@@ -222,16 +224,17 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_listed(const Glo
             idx = prev.y;
         }
         bool pending;
-        const float e = encode_warp_ex<L, false>(w, row, p, active, c0, c1, idx, pending);
+        const float e = encode_warp_ex<L, DEFER>(w, row, p, active, c0, c1, idx, pending);
         if (active) {
             d.out[b] = make_uint2(c0 | (c1 << 16), idx);
             if (d.errors) d.errors[b] = e;
+            if (DEFER) st[b] = RefineSlot{e, pending ? 1u : 0u};
         }
     }
 }
 
 constexpr int L = ICBC_LEVEL;
-constexpr bool kCompact = L >= 2 && L <= 5;
+constexpr bool kCompact = Level<L>::cluster;
 
 // CTAs for n blocks, from the level's launch shape: every warp takes
 // groups_per_warp groups of 32 blocks; a persistent grid is exactly the
@@ -313,27 +316,40 @@ static bool use_byte_rows(const ImageDesc &d) { return Level<L>::cluster && d.we
 
 static int g_resident_trivial = 0, g_resident_listed = 0;
 
-// The two passes of kCompact levels, with the list in stream-ordered scratch.
+// The two passes of kCompact levels, with the list (and at level 9 the
+// refinement hand-over, unless the caller gives one) in stream-ordered
+// scratch; level 9 then runs its refinement pass over every block.
 static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
-                                          cudaStream_t stream, int sms) {
+                                          cudaStream_t stream, int sms, RefineSlot *ext_st,
+                                          unsigned long long *ext_counter) {
     const size_t smem = smem_bytes_byte_rows();
-    cudaError_t e = cudaFuncSetAttribute(k_image_listed<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_image_listed<L, kDefer>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && !g_resident_listed) {
         int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_image_listed<L>, kWarpsPerCta * 32, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_image_listed<L, kDefer>, kWarpsPerCta * 32, smem);
         g_resident_listed = per_sm > 0 ? per_sm : 1;
     }
     if (e != cudaSuccess) return e;
     const size_t list_bytes = ((size_t)d.nblocks * 4 + 15) / 16 * 16;
+    const size_t slot_bytes = (kDefer && !ext_st) ? ((size_t)d.nblocks * sizeof(RefineSlot) + 15) / 16 * 16 + 16 : 0;
     void *scratch = nullptr;
-    e = scratch_alloc(&scratch, list_bytes + 16, stream);
+    e = scratch_alloc(&scratch, list_bytes + 16 + slot_bytes, stream);
     if (e != cudaSuccess) return e;
-    uint32_t *list = static_cast<uint32_t *>(scratch);
-    unsigned int *listed = reinterpret_cast<unsigned int *>(static_cast<char *>(scratch) + list_bytes);
+    char *base = static_cast<char *>(scratch);
+    uint32_t *list = reinterpret_cast<uint32_t *>(base);
+    unsigned int *listed = reinterpret_cast<unsigned int *>(base + list_bytes);
+    RefineSlot *st = ext_st;
+    unsigned long long *counter = ext_counter;
+    if (kDefer && !ext_st) {
+        st = reinterpret_cast<RefineSlot *>(base + list_bytes + 16);
+        counter = reinterpret_cast<unsigned long long *>(base + list_bytes + 16 + slot_bytes - 16);
+    }
     e = cudaMemsetAsync(listed, 0, sizeof(unsigned int), stream);
+    if (e == cudaSuccess && kDefer) e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
     if (e == cudaSuccess) {
         const int grid = grid_for(k_image_trivial<L>, d.nblocks, sms, 0, g_resident_trivial);
-        k_image_trivial<L><<<grid, kWarpsPerCta * 32, 0, stream>>>(G, d, p, list, listed);
+        k_image_trivial<L><<<grid, kWarpsPerCta * 32, 0, stream>>>(G, d, p, list, listed, kDefer ? st : nullptr);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -341,9 +357,10 @@ static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc
         const int64_t most = ((int64_t)d.nblocks + 32 * kWarpsPerCta - 1) / (32 * kWarpsPerCta);
         const int64_t cap = (int64_t)sms * g_resident_listed;
         const int grid = (int)(most < cap ? most : cap);
-        k_image_listed<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed);
+        k_image_listed<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed, st);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess && kDefer) e = launch_refine(G, &d, nullptr, p, d.out, d.errors, st, d.nblocks, counter, stream, sms);
     const cudaError_t f = scratch_free(scratch, stream);
     return e != cudaSuccess ? e : f;
 }
@@ -351,7 +368,8 @@ static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc
 static cudaError_t launch_image(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p, cudaStream_t stream,
                                 int sms, RefineSlot *ext_st, unsigned long long *ext_counter) {
     if constexpr (kCompact) {
-        if (use_byte_rows(d) && d.nblocks < (int64_t(1) << 32)) return launch_image_compacted(G, d, p, stream, sms);
+        if (use_byte_rows(d) && d.nblocks < (int64_t(1) << 32))
+            return launch_image_compacted(G, d, p, stream, sms, ext_st, ext_counter);
     }
     if constexpr (Level<L>::cluster) {
         if (use_byte_rows(d))
