@@ -67,17 +67,17 @@ TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum per level cal
 
 
 def launches_per_level(level: int) -> int:
-    """Kernel launches of one level call on the RGBA8 image: levels 2-5 run in
-    two passes (trivial blocks, then the listed rest), level 9 adds its
-    refinement pass."""
-    return 2 if 2 <= level <= 5 or level == 9 else 1
+    """Kernel launches of one level call on the RGBA8 image: levels 2-9 run in
+    two passes (blocks of 0 or 1 colours, then the listed rest), level 9 adds
+    its refinement pass."""
+    return 1 if level < 2 else 3 if level == 9 else 2
 
 
 def level_kernels(level: int) -> str:
     """The launches of one level call on the RGBA8 image with alpha weights."""
     if level < 2:
         return "k_encode_image<%d>" % level
-    return "k_encode_image_bytes<%d>" % level + (" + k_refine<1>" if level == 9 else "")
+    return "k_image_trivial<%d> + k_image_listed<%d>" % (level, level) + (" + k_refine<1>" if level == 9 else "")
 
 
 def algorithmic_ops(stats: dict, level: int) -> float:
