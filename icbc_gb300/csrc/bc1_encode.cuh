@@ -850,6 +850,52 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 // returned error is the one refinement starts from.
 __device__ __forceinline__ FloatRow float_row(const WarpCtx &w) { return FloatRow{w.in + w.lane * kInStride}; }
 
+// reduce_colors (icbc.h:1683-1728) followed only while at most one colour is
+// kept: true when the block reduces to 0 or 1 colours (`count`, and `c` the
+// colour -- reduce_colors' arithmetic, every texel merged into the first
+// colour), false as soon as a second colour appears.  Unrolled: a row over a
+// register array stays in registers.
+template <class Row>
+__device__ __forceinline__ bool reduce_to_one(const Row &row, float threshold, V3 &c, int &count) {
+    c = v3(0.0f, 0.0f, 0.0f);
+    float wc = 0.0f;
+    count = 0;
+    bool other = false;
+#pragma unroll
+    for (int t = 0; t < 16; t++) {
+        const V3 ct = row.color(t);
+        const float wt = row.weight(t);
+        if (!other && wt > 0) {
+            if (count == 0) {
+                c = ct;
+                wc = wt;
+                count = 1;
+            } else if (near3(c, ct, threshold)) {
+                const float s = wc + wt;
+                c = v3((c.x * wc + ct.x * wt) / s, (c.y * wc + ct.y * wt) / s, (c.z * wc + ct.z * wt) / s);
+                wc = s;
+            } else {
+                other = true;
+            }
+        }
+    }
+    return !other;
+}
+
+// The reduce_colors threshold of a level given at run time (Level<L>::threshold).
+__device__ __forceinline__ float level_threshold(int level) {
+    switch (level) {
+        case 2: return Level<2>::threshold;
+        case 3: return Level<3>::threshold;
+        case 4: return Level<4>::threshold;
+        case 5: return Level<5>::threshold;
+        case 6: return Level<6>::threshold;
+        case 7: return Level<7>::threshold;
+        case 8: return Level<8>::threshold;
+        default: return Level<9>::threshold;
+    }
+}
+
 // The blocks of 0 or 1 reduced colours (icbc.h:3752-3764): the zero block, or
 // the optimal single-colour endpoints of `color` with their error.
 template <int UNROLL = 1, class Row>

@@ -65,25 +65,44 @@ ICBC_DECLARE_LEVEL(9)
 // With refine_base (one entry per image; -1: refine inline) a level-9 image's
 // refinement is deferred: block b's RefineSlot goes to slots[refine_base[i] + b]
 // and launch_refine_batch finishes it.  NULL refine_base: all inline.
+// The blocks the first pass of a two-pass batch left to the second: image
+// i's are list[list_base[i] .. list_base[i] + listed[i]) (list_base[i] < 0:
+// the image is not in two passes and its tasks cover its blocks in order).
+struct BatchLists {
+    uint32_t *list;
+    unsigned int *listed;
+    const int64_t *list_base;
+};
+
 // byte_rows: the kernel with byte texel rows (no image of the batch has a
-// weight plane), four CTAs per SM; else float rows.
+// weight plane), four CTAs per SM; else float rows.  With lists.list, the
+// tasks of listed images take their blocks from the lists.
 cudaError_t launch_encode_batch_float(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
                                       const uint32_t *task_start, int n_images, int ntasks, int *counter,
-                                      cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots);
+                                      cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots,
+                                      BatchLists lists);
 cudaError_t launch_encode_batch_bytes(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
                                       const uint32_t *task_start, int n_images, int ntasks, int *counter,
-                                      cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots);
+                                      cudaStream_t stream, int grid, const int64_t *refine_base, RefineSlot *slots,
+                                      BatchLists lists);
 int batch_ctas_per_sm_float();
 int batch_ctas_per_sm_bytes();
 inline cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
                                        const uint32_t *task_start, int n_images, int ntasks, int *counter,
                                        cudaStream_t stream, int grid, const int64_t *refine_base = nullptr,
-                                       RefineSlot *slots = nullptr, bool byte_rows = false) {
+                                       RefineSlot *slots = nullptr, bool byte_rows = false,
+                                       BatchLists lists = BatchLists{nullptr, nullptr, nullptr}) {
     return byte_rows ? launch_encode_batch_bytes(G, images, tasks, task_start, n_images, ntasks, counter, stream, grid,
-                                                 refine_base, slots)
+                                                 refine_base, slots, lists)
                      : launch_encode_batch_float(G, images, tasks, task_start, n_images, ntasks, counter, stream, grid,
-                                                 refine_base, slots);
+                                                 refine_base, slots, lists);
 }
+// First pass of a two-pass batch (byte rows): finishes the blocks of 0 or 1
+// reduced colours of the images with list_base >= 0 (level-9 ones with an
+// empty refinement slot) and lists the rest.  A grid stride over `tasks`.
+cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
+                                 BatchLists lists, const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream,
+                                 int sms);
 inline int batch_ctas_per_sm(bool byte_rows = false) {
     return byte_rows ? batch_ctas_per_sm_bytes() : batch_ctas_per_sm_float();
 }

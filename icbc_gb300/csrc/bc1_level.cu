@@ -157,27 +157,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 6) k_image_trivial(const Gl
             uint32_t px[16];
             fetch_image_block(d, b, px);
             const ByteRow row{px, lut, alpha};
-            V3 c = v3(0.0f, 0.0f, 0.0f);
-            float wc = 0.0f;
-            int count = 0;
-#pragma unroll
-            for (int t = 0; t < 16; t++) {
-                const V3 ct = row.color(t);
-                const float wt = row.weight(t);
-                if (!other && wt > 0) {
-                    if (count == 0) {
-                        c = ct;
-                        wc = wt;
-                        count = 1;
-                    } else if (near3(c, ct, Level<L>::threshold)) {
-                        const float s = wc + wt;
-                        c = v3((c.x * wc + ct.x * wt) / s, (c.y * wc + ct.y * wt) / s, (c.z * wc + ct.z * wt) / s);
-                        wc = s;
-                    } else {
-                        other = true;
-                    }
-                }
-            }
+            V3 c;
+            int count;
+            other = !reduce_to_one(row, Level<L>::threshold, c, count);
             if (!other) {
                 uint32_t c0, c1, idx;
                 const float e = trivial_block<16>(D, lut, row, p, c, count, c0, c1, idx);

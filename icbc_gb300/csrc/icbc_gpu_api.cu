@@ -302,6 +302,13 @@ struct icbc_gpu_batch {
     unsigned long long *d_refine_counter = nullptr;
     int64_t refine_total = 0;
     int map_n = 0;
+    // Two passes (byte rows): per-image list regions of the level-2..9
+    // images (base -1: none), their counts, and how many leading tasks are
+    // those images' (the planner puts them first).
+    uint32_t *d_list = nullptr;
+    unsigned int *d_listed = nullptr;
+    int64_t *d_list_base = nullptr;
+    int ntasks_listed = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -523,6 +530,23 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     B->grid = sm_count() * batch_ctas_per_sm(byte_rows);
     B->refine_total = refine_total;
     B->map_n = (int)map_image.size();
+    // Byte-row batches run in two passes: the blocks of 0 or 1 reduced
+    // colours of the level-2..9 images are finished by a register-only pass,
+    // which lists the others per image for the encoder.  Those images' tasks
+    // are the leading ones (their levels cost the most).
+    std::vector<int64_t> list_base((size_t)n_images, -1);
+    int64_t list_total = 0;
+    if (byte_rows) {
+        for (const BatchTask &t : tasks) {
+            if (descs[t.image].level < 2) break;
+            B->ntasks_listed++;
+        }
+        for (int i : order) {
+            if (descs[i].level < 2 || descs[i].nblocks == 0 || descs[i].nblocks >= kOwnLaunchBlocks) continue;
+            list_base[i] = list_total;
+            list_total += descs[i].nblocks;
+        }
+    }
     cudaError_t e = cudaMalloc(&B->d_images, sizeof(ImageDesc) * std::max(1, n_images));
     if (e == cudaSuccess) e = cudaMalloc(&B->d_tasks, sizeof(BatchTask) * std::max<size_t>(1, tasks.size()));
     if (e == cudaSuccess) e = cudaMalloc(&B->d_counter, sizeof(int));
@@ -548,16 +572,31 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
             e = cudaMemcpy(B->d_map_image, map_image.data(), sizeof(uint32_t) * map_image.size(),
                            cudaMemcpyHostToDevice);
     }
-    // Capture "reset the queue counter, run the persistent kernel" (and the
-    // level-9 refinement pass after it) once.
+    if (e == cudaSuccess && list_total) {
+        e = cudaMalloc(&B->d_list, sizeof(uint32_t) * (size_t)list_total);
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_listed, sizeof(unsigned int) * n_images);
+        if (e == cudaSuccess) e = cudaMalloc(&B->d_list_base, sizeof(int64_t) * n_images);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(B->d_list_base, list_base.data(), sizeof(int64_t) * n_images, cudaMemcpyHostToDevice);
+    }
+    const BatchLists lists{B->d_list, B->d_listed, B->d_list_base};
+    // Capture "reset the queue counter, run the persistent kernel" (after
+    // the first pass, when there is one; the level-9 refinement pass after
+    // it) once.
     cudaStream_t cs = nullptr;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int), cs);
+        if (e1 == cudaSuccess && B->d_list) {
+            e1 = cudaMemsetAsync(B->d_listed, 0, sizeof(unsigned int) * n_images, cs);
+            if (e1 == cudaSuccess)
+                e1 = launch_batch_trivial(G, B->d_images, B->d_tasks, B->ntasks_listed, lists, B->d_refine_base,
+                                          B->d_slots, cs, sm_count());
+        }
         cudaError_t e2 = e1 == cudaSuccess && B->ntasks
                              ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter,
-                                                   cs, B->grid, B->d_refine_base, B->d_slots, byte_rows)
+                                                   cs, B->grid, B->d_refine_base, B->d_slots, byte_rows, lists)
                              : e1;
         if (e2 == cudaSuccess && refine_total) {
             e2 = cudaMemsetAsync(B->d_refine_counter, 0, sizeof(unsigned long long), cs);
@@ -605,6 +644,9 @@ int icbc_gpu_batch_destroy(icbc_gpu_batch *batch) {
     if (batch->d_map_image) cudaFree(batch->d_map_image);
     if (batch->d_slots) cudaFree(batch->d_slots);
     if (batch->d_refine_counter) cudaFree(batch->d_refine_counter);
+    if (batch->d_list) cudaFree(batch->d_list);
+    if (batch->d_listed) cudaFree(batch->d_listed);
+    if (batch->d_list_base) cudaFree(batch->d_list_base);
     delete batch;
     return ICBC_GPU_OK;
 }

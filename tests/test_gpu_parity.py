@@ -328,7 +328,7 @@ def test_concurrent_calls_on_own_streams(gpu_lib):
 
 
 def test_two_pass_levels_edge_cases(gpu_lib):
-    """Levels 2-5 list the blocks of two or more reduced colours in a first
+    """Levels 2-9 list the blocks of two or more reduced colours in a first
     pass: an image with none (flat), one with all (noise) and a mixed one with
     partial edge blocks all equal the oracle, blocks and errors."""
     ig = gpu_lib
@@ -338,11 +338,60 @@ def test_two_pass_levels_edge_cases(gpu_lib):
     mixed = synth.quality_sweep_image(101, 67, seed=5)
     for img in (flat, noise, mixed):
         dev = _to_dev(img)
-        for level in (2, 3, 4, 5):
+        for level in range(2, 10):
             out, err = ig.compress_image(dev, level, 1, (0.299, 0.587, 0.114), ig.WEIGHTS_ALPHA, with_errors=True)
             ob, oe = O.encode_image(img, level, 1, (0.299, 0.587, 0.114), 1, None, True, True, nthreads=8)
             assert np.array_equal(out.cpu().numpy(), ob), (img.shape, level)
             assert same_bits(err.cpu().numpy(), oe), (img.shape, level)
+
+
+def test_two_pass_batch_edge_cases(gpu_lib):
+    """A batch without weight planes finishes the blocks of 0 or 1 reduced
+    colours of its level-2..9 images in a first pass and lists the others per
+    image for the encoder: flat images (empty lists), noise (every block
+    listed), mixed ones and level-0/1 images in the same batch equal the plain
+    launches, blocks and errors, on two launches; a subset equals the oracle."""
+    import torch
+    ig = gpu_lib
+    rng = np.random.default_rng(23)
+    sources = [np.full((36, 52, 4), 200, np.uint8), rng.integers(0, 256, (40, 44, 4), dtype=np.uint8),
+               synth.quality_sweep_image(101, 67, seed=9), np.full((1, 1, 4), 7, np.uint8),
+               synth.quality_sweep_image(5, 3, seed=10)]
+    cases, devs = [], []
+    for i in range(30):
+        img = sources[i % len(sources)]
+        cases.append(dict(img=img, level=i % 10, decoder=i % 4, cw=(1.0, 1.0, 1.0) if i % 2 else (0.299, 0.587, 0.114),
+                          wm=ig.WEIGHTS_ALPHA if i % 3 == 0 else ig.WEIGHTS_UNIFORM, tcm=bool(i % 4), tcb=bool(i % 7)))
+        devs.append(_to_dev(img))
+    outs, errs, descs = [], [], []
+    for c, dev in zip(cases, devs):
+        nb = ig.blocks_of(c["img"].shape[1], c["img"].shape[0])
+        outs.append(torch.zeros((nb, 8), dtype=torch.uint8, device="cuda"))
+        errs.append(torch.zeros(nb, dtype=torch.float32, device="cuda"))
+        descs.append(ig.image_desc(dev, c["level"], outs[-1], errs[-1], c["decoder"], c["cw"], c["wm"], None,
+                                   c["tcm"], c["tcb"]))
+    plain = []
+    for c, dev in zip(cases, devs):
+        pe = torch.zeros(ig.blocks_of(c["img"].shape[1], c["img"].shape[0]), dtype=torch.float32, device="cuda")
+        po = ig.compress_image(dev, c["level"], c["decoder"], c["cw"], c["wm"], None, c["tcm"], c["tcb"], errors=pe)
+        plain.append((po.cpu().numpy(), pe.cpu().numpy()))
+    batch = ig.Batch(descs)
+    for _ in range(2):
+        for o, e in zip(outs, errs):
+            o.zero_()
+            e.zero_()
+        batch.launch()
+        torch.cuda.synchronize()
+        for c, out, err, (po, pe) in zip(cases, outs, errs, plain):
+            key = (c["img"].shape, c["level"], c["decoder"])
+            assert np.array_equal(out.cpu().numpy(), po), key
+            assert same_bits(err.cpu().numpy(), pe), key
+    batch.close()
+    for c, out, err in list(zip(cases, outs, errs))[::4]:
+        ob, oe = O.encode_image(c["img"], c["level"], c["decoder"], c["cw"], c["wm"], None, c["tcm"], c["tcb"],
+                                nthreads=8)
+        assert np.array_equal(out.cpu().numpy(), ob), (c["img"].shape, c["level"])
+        assert same_bits(err.cpu().numpy(), oe), (c["img"].shape, c["level"])
 
 
 def test_decode_evaluate_golden(gpu_lib):
