@@ -58,12 +58,14 @@ REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
 
 
 # DRAM bytes per level call (dram__bytes_read.sum + dram__bytes_write.sum of
-# its launches) from one ncu capture of this workload, summarised in
-# profiles/k_encode_image_bytes_L8_L9_k_refine_quality_sweep_4096.md.  Level 9
-# is the encoder plus the refinement pass; each reads the 64 MB image.
-NCU_TRAFFIC_BYTES = {8: 75.66e6 + 1.59e6, 9: (75.64e6 + 3.35e6) + (75.96e6 + 2.18e6)}
+# its launches, cold-cache) from one ncu capture of this workload, summarised
+# in profiles/k_image_listed_L8_L9_k_refine_quality_sweep_4096.md: the first
+# pass, the listed pass and, at level 9, the refinement pass; each reads the
+# texels of the blocks it handles.
+NCU_TRAFFIC_BYTES = {8: (67.18e6 + 2.05e6) + (70.94e6 + 1.47e6),
+                     9: (67.47e6 + 2.74e6) + (70.97e6 + 2.16e6) + (76.00e6 + 2.03e6)}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum per level call, " \
-                 "profiles/k_encode_image_bytes_L8_L9_k_refine_quality_sweep_4096.md"
+                 "profiles/k_image_listed_L8_L9_k_refine_quality_sweep_4096.md"
 
 
 def launches_per_level(level: int) -> int:
