@@ -23,12 +23,28 @@ __device__ __forceinline__ float encode_task(const WarpCtx &w, const ImageDesc &
     return encode_warp_ex<L, DEFER>(w, float_row(w), p, active, c0, c1, idx, pending);
 }
 
+// Task t of a batch: an entry of the explicit list, or -- without one --
+// found from per-image offsets: task t belongs to the last image whose first
+// task (`task_start[i]`, n_images + 1 entries) is <= t.
+__device__ __forceinline__ BatchTask batch_task(const BatchTask *tasks, const uint32_t *task_start, int n_images,
+                                                int t) {
+    if (tasks) return tasks[t];
+    int lo = 0, hi = n_images;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)task_start[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    BatchTask task;
+    task.image = (uint32_t)lo;
+    task.first_block = (uint32_t)(t - (int)task_start[lo]) * 32u;
+    return task;
+}
+
 // Persistent batched encoder: every warp takes the next task (32 blocks of
 // one image) from an atomic counter until the queue is empty.  Tasks are
-// ordered most expensive level first by the planner.  A task is either an
-// entry of an explicit list (`tasks`), or -- when `tasks` is NULL -- found from
-// per-image offsets: task t belongs to the last image whose first task
-// (`task_start[i]`, n_images + 1 entries) is <= t.  With `refine_base`, the
+// ordered most expensive level first by the planner (batch_task: an explicit
+// list, or per-image offsets).  With `refine_base`, the
 // level-9 images leave refinement to k_refine's batch mode (bc1_refine.cu),
 // which runs after this kernel in the same stream: the same split as the
 // plain level-9 launches, so lanes do not wait for each other's refinement.
@@ -50,19 +66,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, BYTES ? 4 : 1)
         if (lane == 0) t = atomicAdd(counter, 1);
         t = __shfl_sync(kFull, t, 0);
         if (t >= ntasks) break;
-        BatchTask task;
-        if (tasks) {
-            task = tasks[t];
-        } else {
-            int lo = 0, hi = n_images;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if ((int)task_start[mid] <= t) lo = mid;
-                else hi = mid;
-            }
-            task.image = (uint32_t)lo;
-            task.first_block = (uint32_t)(t - (int)task_start[lo]) * 32u;
-        }
+        const BatchTask task = batch_task(tasks, task_start, n_images, t);
         const ImageDesc &d = images[task.image];
         const int level = d.level;
         const int64_t lb = lists.list ? lists.list_base[task.image] : -1;
@@ -130,14 +134,14 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, BYTES ? 4 : 1)
 // any other goes to its image's list with one atomic per warp.  Only the u8
 // table is in shared memory, so six CTAs fit on an SM.
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 6)
-    k_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
-                    BatchLists lists, const int64_t *refine_base, RefineSlot *slots) {
+    k_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, const uint32_t *task_start,
+                    int n_images, int ntasks, BatchLists lists, const int64_t *refine_base, RefineSlot *slots) {
     __shared__ float lut[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = G->s.lut255[i];
     __syncthreads();
     const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5); t < ntasks; t += gridDim.x * kWarpsPerCta) {
-        const BatchTask task = tasks[t];
+        const BatchTask task = batch_task(tasks, task_start, n_images, t);
         const int64_t lb = lists.list_base[task.image];
         if (lb < 0) continue;
         const ImageDesc &d = images[task.image];
@@ -175,9 +179,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 6)
     }
 }
 
-cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
-                                 BatchLists lists, const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream,
-                                 int sms) {
+cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                 const uint32_t *task_start, int n_images, int ntasks, BatchLists lists,
+                                 const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream, int sms) {
     if (ntasks <= 0) return cudaSuccess;
     static int resident = 0;
     if (!resident &&
@@ -188,7 +192,8 @@ cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images,
     const int64_t need = ((int64_t)ntasks + kWarpsPerCta - 1) / kWarpsPerCta;
     const int64_t cap = (int64_t)sms * resident;
     const int grid = (int)(need < cap ? need : cap);
-    k_batch_trivial<<<grid, kWarpsPerCta * 32, 0, stream>>>(G, images, tasks, ntasks, lists, refine_base, slots);
+    k_batch_trivial<<<grid, kWarpsPerCta * 32, 0, stream>>>(G, images, tasks, task_start, n_images, ntasks, lists,
+                                                            refine_base, slots);
     return cudaGetLastError();
 }
 #endif

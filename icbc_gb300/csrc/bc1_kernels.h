@@ -99,10 +99,11 @@ inline cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *i
 }
 // First pass of a two-pass batch (byte rows): finishes the blocks of 0 or 1
 // reduced colours of the images with list_base >= 0 (level-9 ones with an
-// empty refinement slot) and lists the rest.  A grid stride over `tasks`.
-cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int ntasks,
-                                 BatchLists lists, const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream,
-                                 int sms);
+// empty refinement slot) and lists the rest.  A grid stride over the first
+// ntasks tasks (`tasks`, or per-image offsets as for launch_encode_batch).
+cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                 const uint32_t *task_start, int n_images, int ntasks, BatchLists lists,
+                                 const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream, int sms);
 inline int batch_ctas_per_sm(bool byte_rows = false) {
     return byte_rows ? batch_ctas_per_sm_bytes() : batch_ctas_per_sm_float();
 }

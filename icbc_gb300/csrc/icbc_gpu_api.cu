@@ -591,8 +591,8 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
         if (e1 == cudaSuccess && B->d_list) {
             e1 = cudaMemsetAsync(B->d_listed, 0, sizeof(unsigned int) * n_images, cs);
             if (e1 == cudaSuccess)
-                e1 = launch_batch_trivial(G, B->d_images, B->d_tasks, B->ntasks_listed, lists, B->d_refine_base,
-                                          B->d_slots, cs, sm_count());
+                e1 = launch_batch_trivial(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks_listed, lists,
+                                          B->d_refine_base, B->d_slots, cs, sm_count());
         }
         cudaError_t e2 = e1 == cudaSuccess && B->ntasks
                              ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter,

@@ -10,6 +10,9 @@
 // copies its blocks to pinned staging; a host callback marks the launch done
 // and the scheduler hands the blocks to the callers' buffers and frees the
 // space.  No waits on the device side: the kernel drains a finite queue.
+// A launch runs in the batched form's two passes: the blocks of 0 or 1
+// reduced colours of level-2..9 requests are finished by a register-only
+// pass, which lists the others in the request's own arena space.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -92,7 +95,7 @@ struct Request {
     icbc_gpu_request r{};
     ImageDesc d{};
     int64_t dpitch = 0;
-    size_t dev_off = 0, dev_bytes = 0, out_off = 0, err_off = 0;
+    size_t dev_off = 0, dev_bytes = 0, out_off = 0, err_off = 0, list_off = 0;
     size_t host_off = 0, host_bytes = 0;
     size_t in_off = 0, in_bytes = 0;  // pinned copy of the texels (rows at dpitch)
     bool staged = false;
@@ -106,6 +109,11 @@ struct Slot {
     int *d_counter = nullptr;
     ImageDesc *h_images = nullptr;   // pinned
     uint32_t *h_start = nullptr;     // pinned
+    // Two passes: each request's list (base in 4-byte entries from the arena
+    // start; -1 below level 2) and its count.
+    int64_t *d_list_base = nullptr;
+    int64_t *h_list_base = nullptr;  // pinned
+    unsigned int *d_listed = nullptr;
     std::vector<Request *> reqs;
     bool busy = false;
     int status = ICBC_GPU_OK;
@@ -152,7 +160,9 @@ void size_request(icbc_gpu_server *S, Request *q) {
     const size_t img = round_up((size_t)q->dpitch * q->r.height, kGranule);
     const size_t out = round_up((size_t)nb * 8, kGranule);
     const size_t err = q->r.errors ? round_up((size_t)nb * 4, kGranule) : 0;
-    q->dev_bytes = img + out + err;
+    const size_t list = q->d.level >= 2 ? round_up((size_t)nb * 4, kGranule) : 0;
+    q->list_off = img + out + err;
+    q->dev_bytes = img + out + err + list;
     q->host_bytes = out + err;
     (void)S;
 }
@@ -172,7 +182,7 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
         return level_cost(a->r.level) > level_cost(b->r.level);
     });
     cudaError_t e = cudaSuccess;
-    uint32_t total = 0;
+    uint32_t total = 0, listed_tasks = 0;  // level-2..9 requests come first: their tasks lead
     for (size_t i = 0; i < reqs.size() && e == cudaSuccess; i++) {
         Request *q = reqs[i];
         uint8_t *base = S->d_arena + q->dev_off;
@@ -191,16 +201,27 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
         if (e == cudaSuccess && d.level >= 4) e = cudaMemsetAsync(d.out, 0, (size_t)d.nblocks * 8, slot.stream);
         slot.h_images[i] = d;
         slot.h_start[i] = total;
+        slot.h_list_base[i] = d.level >= 2 && d.nblocks > 0 ? (int64_t)((q->dev_off + q->list_off) / 4) : -1;
+        if (d.level >= 2) listed_tasks = total + (uint32_t)((d.nblocks + 31) / 32);
         total += (uint32_t)((d.nblocks + 31) / 32);
     }
     slot.h_start[reqs.size()] = total;
     const int n = (int)reqs.size();
+    const BatchLists lists{reinterpret_cast<uint32_t *>(S->d_arena), slot.d_listed, slot.d_list_base};
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(slot.d_images, slot.h_images, sizeof(ImageDesc) * n, cudaMemcpyHostToDevice, slot.stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(slot.d_start, slot.h_start, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice,
                             slot.stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(slot.d_counter, 0, sizeof(int), slot.stream);
+    if (e == cudaSuccess && listed_tasks) {
+        e = cudaMemcpyAsync(slot.d_list_base, slot.h_list_base, sizeof(int64_t) * n, cudaMemcpyHostToDevice,
+                            slot.stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(slot.d_listed, 0, sizeof(unsigned int) * n, slot.stream);
+        if (e == cudaSuccess)
+            e = launch_batch_trivial(S->G, slot.d_images, nullptr, slot.d_start, n, (int)listed_tasks, lists, nullptr,
+                                     nullptr, slot.stream, current_sm_count());
+    }
     if (e == cudaSuccess)
         // A persistent grid no larger than the batch's work (four tasks per
         // CTA at least), so small batches share the GPU instead of each
@@ -208,7 +229,7 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
         // Requests carry uniform or alpha weights: the byte-row kernel.
         e = launch_encode_batch(S->G, slot.d_images, nullptr, slot.d_start, n, (int)total, slot.d_counter,
                                 slot.stream, (int)std::min<uint32_t>((uint32_t)S->grid, (total + 3) / 4), nullptr,
-                                nullptr, true);
+                                nullptr, true, listed_tasks ? lists : BatchLists{nullptr, nullptr, nullptr});
     for (size_t i = 0; i < reqs.size() && e == cudaSuccess; i++) {
         Request *q = reqs[i];
         const ImageDesc &d = slot.h_images[i];
@@ -354,6 +375,9 @@ int icbc_gpu_server_create(const icbc_gpu_server_config *config, icbc_gpu_server
         if (e == cudaSuccess) e = cudaMalloc(&slot.d_counter, sizeof(int));
         if (e == cudaSuccess) e = cudaMallocHost(&slot.h_images, sizeof(ImageDesc) * n);
         if (e == cudaSuccess) e = cudaMallocHost(&slot.h_start, sizeof(uint32_t) * (n + 1));
+        if (e == cudaSuccess) e = cudaMalloc(&slot.d_list_base, sizeof(int64_t) * n);
+        if (e == cudaSuccess) e = cudaMalloc(&slot.d_listed, sizeof(unsigned int) * n);
+        if (e == cudaSuccess) e = cudaMallocHost(&slot.h_list_base, sizeof(int64_t) * n);
     }
     if (e != cudaSuccess) {
         icbc_gpu_server_destroy(S);
@@ -523,6 +547,9 @@ int icbc_gpu_server_destroy(icbc_gpu_server *S) {
         if (slot.d_counter) cudaFree(slot.d_counter);
         if (slot.h_images) cudaFreeHost(slot.h_images);
         if (slot.h_start) cudaFreeHost(slot.h_start);
+        if (slot.d_list_base) cudaFree(slot.d_list_base);
+        if (slot.d_listed) cudaFree(slot.d_listed);
+        if (slot.h_list_base) cudaFreeHost(slot.h_list_base);
     }
     if (S->d_arena) cudaFree(S->d_arena);
     if (S->h_stage) cudaFreeHost(S->h_stage);

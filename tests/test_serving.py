@@ -59,6 +59,26 @@ def test_alone_equals_mix_equals_plain(gpu_lib):
         srv.close()
 
 
+def test_two_pass_edge_requests(gpu_lib):
+    """Launches finish the blocks of 0 or 1 reduced colours of level-2..9
+    requests first and list the rest: flat requests (empty lists), noise
+    (every block listed) and ragged sizes at every level, in one mix, equal
+    the plain launches."""
+    rng = np.random.default_rng(31)
+    imgs = [np.full((20, 36, 4), 90, np.uint8), rng.integers(0, 256, (28, 20, 4), dtype=np.uint8),
+            synth.quality_sweep_image(37, 29, seed=4), np.full((1, 1, 4), 3, np.uint8)]
+    reqs = [(imgs[i % 4], i % 10, i % 3) for i in range(40)]
+    srv = ig.Server(64 << 20, max_inflight=2, max_batch_images=24)
+    try:
+        ids = [srv.submit(img, lv, dec) for img, lv, dec in reqs]
+        for rid in ids:
+            assert srv.wait(rid, 20000) == 0
+        for (img, lv, dec), rid in zip(reqs, ids):
+            assert np.array_equal(srv.result(rid)[0], _plain(img, lv, dec)), (img.shape, lv, dec)
+    finally:
+        srv.close()
+
+
 def test_budget_backpressure_and_rejection(gpu_lib):
     budget = 1 << 20  # 1 MiB: only a few small requests fit at once
     srv = ig.Server(budget, max_inflight=2, max_batch_images=8)
