@@ -215,7 +215,10 @@ int icbc_gpu_compress_bc1_image_host(const uint8_t *rgba, int32_t width, int32_t
  * Serving form (no counterpart in the reference, which encodes on the
  * caller's thread): a request loop that batches encode requests of any size
  * and level as they arrive.  Texels and blocks are staged in one device arena
- * of hbm_budget_bytes allocated at create; a request is admitted (FIFO) once
+ * of hbm_budget_bytes allocated at create (per request: its texels at rows
+ * of 16-byte multiples, 8 bytes per block, 4 per block for errors if asked,
+ * and 4 per block of working space at levels 2-9, each rounded up to 256
+ * bytes); a request is admitted (FIFO) once
  * its bytes fit in the arena, so requests that arrive while others run join
  * the next batched launch as memory frees up, and up to max_inflight batches
  * run on the GPU at once.  Results equal the single-image encode bit for bit.
