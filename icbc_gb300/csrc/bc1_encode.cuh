@@ -363,21 +363,25 @@ __device__ __forceinline__ uint32_t add565(uint32_t c, int dr, int dg, int db) {
     return (r << 11) | (g << 5) | b;
 }
 
+// Generic nearest-of-four index of one texel (compute_indices' loop body,
+// icbc.h:3179-3235), palette entries already multiplied by the colour weights.
+__device__ __forceinline__ uint32_t index_generic(V3 color, V3 cw, V3 p0, V3 p1, V3 p2, V3 p3) {
+    const V3 c = color * cw;
+    const V3 t0 = c - p0, t1 = c - p1, t2 = c - p2, t3 = c - p3;
+    const float d0 = dot(t0, t0), d1 = dot(t1, t1), d2 = dot(t2, t2), d3 = dot(t3, t3);
+    const bool i1 = (d1 <= d0) & (d1 < d2) & (d1 < d3);
+    const bool i2 = (d2 <= d0) & (d2 <= d1) & (d2 < d3);
+    const bool i3 = (d3 <= d0) & (d3 <= d1) & (d3 <= d2);
+    return (uint32_t)(i1 | i3) | ((uint32_t)(i2 | i3) << 1);
+}
+
 // Generic nearest-of-four indices (compute_indices, icbc.h:3179-3235).
 template <int UNROLL = 1, class Row>
 __device__ __forceinline__ uint32_t indices_generic(const Row &row, V3 cw, const PalF &pal) {
     const V3 p0 = pal.c[0] * cw, p1 = pal.c[1] * cw, p2 = pal.c[2] * cw, p3 = pal.c[3] * cw;
     uint32_t out = 0;
 #pragma unroll UNROLL
-    for (int t = 0; t < 16; t++) {
-        const V3 c = row.color(t) * cw;
-        const V3 t0 = c - p0, t1 = c - p1, t2 = c - p2, t3 = c - p3;
-        const float d0 = dot(t0, t0), d1 = dot(t1, t1), d2 = dot(t2, t2), d3 = dot(t3, t3);
-        const bool i1 = (d1 <= d0) & (d1 < d2) & (d1 < d3);
-        const bool i2 = (d2 <= d0) & (d2 <= d1) & (d2 < d3);
-        const bool i3 = (d3 <= d0) & (d3 <= d1) & (d3 <= d2);
-        out |= ((uint32_t)(i1 | i3) | ((uint32_t)(i2 | i3) << 1)) << (2 * t);
-    }
+    for (int t = 0; t < 16; t++) out |= index_generic(row.color(t), cw, p0, p1, p2, p3) << (2 * t);
     return out;
 }
 
@@ -434,10 +438,15 @@ __device__ __forceinline__ void refine_begin(const WarpCtx &w, const Row &row, c
     s.base_idx = indices_generic<4>(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D));
 }
 
-// Iteration s.i of refine_endpoints (icbc.h:3614-3648), identical to one trip
-// of refine()'s loop.  Returns true when the loop would stop after it.
+// Iteration s.i of refine_endpoints (icbc.h:3614-3648), one trip of
+// refine()'s loop but for its index update: when the step is accepted it
+// takes the candidate and returns true with the candidate's palette in `pr`,
+// and s.base_idx must be set to indices_generic(row, cw, pr) before the next
+// iteration (the caller computes it, across lanes).  `stop`: the loop would
+// stop after this iteration.
 template <class Row>
-__device__ __forceinline__ bool refine_step(const WarpCtx &w, const Row &row, const EncodeParams &p, RefineLane &s) {
+__device__ __forceinline__ bool refine_try(const WarpCtx &w, const Row &row, const EncodeParams &p, RefineLane &s,
+                                           PalF &pr, bool &stop) {
     const int d = s.i & 15;
     const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
     uint32_t r0 = s.c0, r1 = s.c1;
@@ -447,18 +456,19 @@ __device__ __forceinline__ bool refine_step(const WarpCtx &w, const Row &row, co
         if (r0 == r1) r1 = add565(r1, 0, 1, 0);
         if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
     }
-    const PalF pr = palette_f(r0, r1, p.decoder, w.T->lut255, w.D);
+    pr = palette_f(r0, r1, p.decoder, w.T->lut255, w.D);
     const float e = block_error<4>(row, p.cw, pr, s.base_idx);
-    if (e < s.best) {
+    const bool accept = e < s.best;
+    if (accept) {
         s.best = e;
         s.c0 = r0;
         s.c1 = r1;
         s.idx = s.base_idx;
         s.last = s.i;
-        s.base_idx = indices_generic<4>(row, p.cw, pr);
     }
     s.i++;
-    return (s.i - 1 - s.last > 32) || s.i == 256;
+    stop = (s.i - 1 - s.last > 32) || s.i == 256;
+    return accept;
 }
 
 // Per-block hand-over from the encode kernel to the refinement kernel.

@@ -44,6 +44,18 @@ __device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_
 
 constexpr int kRefillBatch = 8;
 
+__device__ __forceinline__ V3 shfl3(V3 v, int src) {
+    return v3(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src));
+}
+
+// Bit t of x (t < 16) to bit 2t.
+__device__ __forceinline__ uint32_t spread_bits(uint32_t x) {
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    return (x | (x << 1)) & 0x55555555u;
+}
+
 // MODE 0: float blocks (s), 1: one image (d), 2: the deferred level-9 blocks
 // of a batch (images + map), each lane with its own image's decoder and
 // parameters.
@@ -64,6 +76,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
     uint2 *o = nullptr;
     float *er = nullptr;
     bool have = false, exhausted = false;
+    // The last accepted candidate's palette times the colour weights, the
+    // source of the index update the warp computes for this lane.
+    V3 q0 = v3(0.0f, 0.0f, 0.0f), q1 = q0, q2 = q0, q3 = q0;
     for (;;) {
         // Lanes without a block take the next ones; blocks that need no
         // refinement are skipped (their error and bytes are final already).
@@ -116,7 +131,37 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
             need = __ballot_sync(kFull, !have && !exhausted);
         }
         if (!__any_sync(kFull, have)) break;
-        if (have && refine_step(w, FloatRow{row}, lp, r)) {
+        bool accepted = false, stop = false;
+        if (have) {
+            PalF pr;
+            accepted = refine_try(w, FloatRow{row}, lp, r, pr, stop);
+            if (accepted) {
+                q0 = pr.c[0] * lp.cw;
+                q1 = pr.c[1] * lp.cw;
+                q2 = pr.c[2] * lp.cw;
+                q3 = pr.c[3] * lp.cw;
+            }
+        }
+        // An accepted step's lane needs indices_generic of its new palette
+        // before its next step.  Each texel's index depends on that texel
+        // alone, so the warp computes them for two such lanes at a time: the
+        // half-warp of lane l takes texel l & 15 of one block, and two ballots
+        // pack the 2-bit indices in texel order.
+        unsigned m = __ballot_sync(kFull, accepted);
+        while (m) {
+            const int l0 = __ffs(m) - 1;
+            m &= m - 1;
+            const int l1 = m ? __ffs(m) - 1 : l0;
+            m &= m - 1;
+            const int src = lane < 16 ? l0 : l1;
+            const V3 p0 = shfl3(q0, src), p1 = shfl3(q1, src), p2 = shfl3(q2, src), p3 = shfl3(q3, src);
+            const V3 cw = shfl3(lp.cw, src);
+            const uint32_t x = index_generic(FloatRow{w.in + src * kInStride}.color(lane & 15), cw, p0, p1, p2, p3);
+            const unsigned lo = __ballot_sync(kFull, x & 1u), hi = __ballot_sync(kFull, x >> 1);
+            if (lane == l0) r.base_idx = spread_bits(lo & 0xffffu) | (spread_bits(hi & 0xffffu) << 1);
+            else if (lane == l1) r.base_idx = spread_bits(lo >> 16) | (spread_bits(hi >> 16) << 1);
+        }
+        if (have && stop) {
             *o = make_uint2(r.c0 | (r.c1 << 16), r.idx);
             if (er) *er = r.best;
             have = false;
