@@ -42,7 +42,7 @@ __device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_
     }
 }
 
-constexpr int kRefillBatch = 8;
+constexpr int kRefillBatch = 16;  // 4: 3% slower, 8: 0.4%, 12: as 16 (hard mixture, level 9)
 
 __device__ __forceinline__ V3 shfl3(V3 v, int src) {
     return v3(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src));
