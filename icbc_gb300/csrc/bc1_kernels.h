@@ -74,6 +74,27 @@ struct BatchLists {
     const int64_t *list_base;
 };
 
+// The batched form's kernel for the tasks task0 .. task0 + ntasks - 1 of a
+// byte-row batch, all of one level (each level's own code, compiled with
+// that level's plain kernels); otherwise as launch_encode_batch.
+using BatchLevelLauncher = cudaError_t (*)(const GlobalTables *, const ImageDesc *, const BatchTask *, int, int, int *,
+                                           cudaStream_t, int, const int64_t *, RefineSlot *, BatchLists);
+#define ICBC_DECLARE_BATCH_LEVEL(L)                                                                                \
+    cudaError_t launch_batch_level_l##L(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,     \
+                                        int task0, int ntasks, int *counter, cudaStream_t stream, int grid,        \
+                                        const int64_t *refine_base, RefineSlot *slots, BatchLists lists);
+ICBC_DECLARE_BATCH_LEVEL(0)
+ICBC_DECLARE_BATCH_LEVEL(1)
+ICBC_DECLARE_BATCH_LEVEL(2)
+ICBC_DECLARE_BATCH_LEVEL(3)
+ICBC_DECLARE_BATCH_LEVEL(4)
+ICBC_DECLARE_BATCH_LEVEL(5)
+ICBC_DECLARE_BATCH_LEVEL(6)
+ICBC_DECLARE_BATCH_LEVEL(7)
+ICBC_DECLARE_BATCH_LEVEL(8)
+ICBC_DECLARE_BATCH_LEVEL(9)
+#undef ICBC_DECLARE_BATCH_LEVEL
+
 // byte_rows: the kernel with byte texel rows (no image of the batch has a
 // weight plane), four CTAs per SM; else float rows.  With lists.list, the
 // tasks of listed images take their blocks from the lists.

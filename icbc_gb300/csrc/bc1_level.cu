@@ -5,7 +5,7 @@
 // add separately rounded, as the reference's scalar build does.
 #include <cuda_runtime.h>
 
-#include "bc1_loaders.cuh"
+#include "bc1_batch_task.cuh"
 
 #ifndef ICBC_LEVEL
 #error "compile with -DICBC_LEVEL=<0..9>"
@@ -215,6 +215,18 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_listed(const Glo
     }
 }
 
+// The batched form's kernel for this level's tasks of a byte-row batch:
+// run_batch with the level fixed, so the kernel holds one level's code as the
+// plain kernels do (the all-levels kernel stalls about twice as often on
+// instruction fetch for the same blocks).
+template <int LV>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
+    k_batch_level(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int task0, int ntasks,
+                  int *counter, const int64_t *refine_base, RefineSlot *slots, BatchLists lists) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    run_batch<true, LV>(G, smem, images, tasks, nullptr, 0, task0, ntasks, counter, refine_base, slots, lists);
+}
+
 constexpr int L = ICBC_LEVEL;
 constexpr bool kCompact = Level<L>::cluster;
 
@@ -377,6 +389,18 @@ cudaError_t ICBC_CAT(launch_blocks_l, ICBC_LEVEL)(const GlobalTables *G, const B
                    k_encode_blocks<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, s, p, o, errors, n, st);
                },
                G, nullptr, &s, p, o, errors);
+}
+
+cudaError_t ICBC_CAT(launch_batch_level_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc *images,
+                                                        const BatchTask *tasks, int task0, int ntasks, int *counter,
+                                                        cudaStream_t stream, int grid, const int64_t *refine_base,
+                                                        RefineSlot *slots, BatchLists lists) {
+    const size_t smem = smem_bytes_byte_rows();
+    cudaError_t e = cudaFuncSetAttribute(k_batch_level<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_batch_level<L><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, images, tasks, task0, ntasks, counter, refine_base,
+                                                               slots, lists);
+    return cudaGetLastError();
 }
 
 cudaError_t ICBC_CAT(launch_image_l, ICBC_LEVEL)(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,

@@ -158,6 +158,10 @@ const ImageLauncherExt kImageLaunchExt[10] = {launch_image_ext_l0, launch_image_
                                               launch_image_ext_l3, launch_image_ext_l4, launch_image_ext_l5,
                                               launch_image_ext_l6, launch_image_ext_l7, launch_image_ext_l8,
                                               launch_image_ext_l9};
+const BatchLevelLauncher kBatchLevelLaunch[10] = {launch_batch_level_l0, launch_batch_level_l1, launch_batch_level_l2,
+                                                  launch_batch_level_l3, launch_batch_level_l4, launch_batch_level_l5,
+                                                  launch_batch_level_l6, launch_batch_level_l7, launch_batch_level_l8,
+                                                  launch_batch_level_l9};
 
 // An image of at least this many blocks (a 4096 x 4096 image) fills the GPU
 // for many waves on its own: inside a batch it gets its level's own kernel,
@@ -549,7 +553,8 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     }
     cudaError_t e = cudaMalloc(&B->d_images, sizeof(ImageDesc) * std::max(1, n_images));
     if (e == cudaSuccess) e = cudaMalloc(&B->d_tasks, sizeof(BatchTask) * std::max<size_t>(1, tasks.size()));
-    if (e == cudaSuccess) e = cudaMalloc(&B->d_counter, sizeof(int));
+    // counter 0: the all-levels kernel's queue; 1 + L: level L's kernel's
+    if (e == cudaSuccess) e = cudaMalloc(&B->d_counter, sizeof(int) * 11);
     if (e == cudaSuccess && n_images)
         e = cudaMemcpy(B->d_images, descs.data(), sizeof(ImageDesc) * n_images, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !tasks.empty())
@@ -580,6 +585,28 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
             e = cudaMemcpy(B->d_list_base, list_base.data(), sizeof(int64_t) * n_images, cudaMemcpyHostToDevice);
     }
     const BatchLists lists{B->d_list, B->d_listed, B->d_list_base};
+    // Byte-row batches run one kernel per level (each level's own code), on
+    // parallel branches of the graph so one level's tail overlaps the next
+    // level's start; the planner's order keeps each level's tasks together.
+    int lv_begin[10], lv_end[10];
+    for (int l = 0; l < 10; l++) lv_begin[l] = lv_end[l] = -1;
+    bool per_level = byte_rows && !tasks.empty();
+    for (size_t t = 0; t < tasks.size() && per_level; t++) {
+        const int l = descs[tasks[t].image].level;
+        if (lv_begin[l] < 0) lv_begin[l] = (int)t;
+        else if (lv_end[l] != (int)t) per_level = false;
+        lv_end[l] = (int)t + 1;
+    }
+    cudaStream_t lv_stream[10] = {};
+    cudaEvent_t fork = nullptr, lv_done[10] = {};
+    if (e == cudaSuccess && per_level) {
+        e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+        for (int l = 0; l < 10 && e == cudaSuccess; l++) {
+            if (lv_begin[l] < 0) continue;
+            e = cudaStreamCreateWithFlags(&lv_stream[l], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&lv_done[l], cudaEventDisableTiming);
+        }
+    }
     // Capture "reset the queue counter, run the persistent kernel" (after
     // the first pass, when there is one; the level-9 refinement pass after
     // it) once.
@@ -587,17 +614,31 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int), cs);
+        cudaError_t e1 = cudaMemsetAsync(B->d_counter, 0, sizeof(int) * 11, cs);
         if (e1 == cudaSuccess && B->d_list) {
             e1 = cudaMemsetAsync(B->d_listed, 0, sizeof(unsigned int) * n_images, cs);
             if (e1 == cudaSuccess)
                 e1 = launch_batch_trivial(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks_listed, lists,
                                           B->d_refine_base, B->d_slots, cs, sm_count());
         }
-        cudaError_t e2 = e1 == cudaSuccess && B->ntasks
-                             ? launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter,
-                                                   cs, B->grid, B->d_refine_base, B->d_slots, byte_rows, lists)
-                             : e1;
+        cudaError_t e2 = e1;
+        if (e2 == cudaSuccess && B->ntasks && per_level) {
+            e2 = cudaEventRecord(fork, cs);
+            for (int l = 9; l >= 0 && e2 == cudaSuccess; l--) {
+                if (lv_begin[l] < 0) continue;
+                const int n = lv_end[l] - lv_begin[l];
+                const int grid = std::min(B->grid, (n + kWarpsPerCta - 1) / kWarpsPerCta);  // a task per warp at most
+                e2 = cudaStreamWaitEvent(lv_stream[l], fork, 0);
+                if (e2 == cudaSuccess)
+                    e2 = kBatchLevelLaunch[l](G, B->d_images, B->d_tasks, lv_begin[l], n, B->d_counter + 1 + l,
+                                              lv_stream[l], grid, B->d_refine_base, B->d_slots, lists);
+                if (e2 == cudaSuccess) e2 = cudaEventRecord(lv_done[l], lv_stream[l]);
+                if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(cs, lv_done[l], 0);
+            }
+        } else if (e2 == cudaSuccess && B->ntasks) {
+            e2 = launch_encode_batch(G, B->d_images, B->d_tasks, nullptr, n_images, B->ntasks, B->d_counter, cs,
+                                     B->grid, B->d_refine_base, B->d_slots, byte_rows, lists);
+        }
         if (e2 == cudaSuccess && refine_total) {
             e2 = cudaMemsetAsync(B->d_refine_counter, 0, sizeof(unsigned long long), cs);
             if (e2 == cudaSuccess)
@@ -617,6 +658,11 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&B->exec, B->graph, 0);
     if (cs) cudaStreamDestroy(cs);
+    for (int l = 0; l < 10; l++) {
+        if (lv_stream[l]) cudaStreamDestroy(lv_stream[l]);
+        if (lv_done[l]) cudaEventDestroy(lv_done[l]);
+    }
+    if (fork) cudaEventDestroy(fork);
     if (e != cudaSuccess) {
         int r = set_cuda_error(e);
         icbc_gpu_batch_destroy(B);
