@@ -426,16 +426,17 @@ struct RefineLane {
     int i, last;
 };
 
+// `lut`: the exact table of i / 255.0f.
 template <class Row>
-__device__ __forceinline__ void refine_begin(const WarpCtx &w, const Row &row, const EncodeParams &p, float error,
-                                             uint32_t c0, uint32_t c1, uint32_t idx, RefineLane &s) {
+__device__ __forceinline__ void refine_begin(const WarpCtx &w, const float *lut, const Row &row, const EncodeParams &p,
+                                             float error, uint32_t c0, uint32_t c1, uint32_t idx, RefineLane &s) {
     s.c0 = c0;
     s.c1 = c1;
     s.idx = idx;
     s.best = error;
     s.i = 0;
     s.last = 0;
-    s.base_idx = indices_generic<4>(row, p.cw, palette_f(c0, c1, p.decoder, w.T->lut255, w.D));
+    s.base_idx = indices_generic<4>(row, p.cw, palette_f(c0, c1, p.decoder, lut, w.D));
 }
 
 // Iteration s.i of refine_endpoints (icbc.h:3614-3648), one trip of
@@ -445,8 +446,8 @@ __device__ __forceinline__ void refine_begin(const WarpCtx &w, const Row &row, c
 // iteration (the caller computes it, across lanes).  `stop`: the loop would
 // stop after this iteration.
 template <class Row>
-__device__ __forceinline__ bool refine_try(const WarpCtx &w, const Row &row, const EncodeParams &p, RefineLane &s,
-                                           PalF &pr, bool &stop) {
+__device__ __forceinline__ bool refine_try(const WarpCtx &w, const float *lut, const Row &row, const EncodeParams &p,
+                                           RefineLane &s, PalF &pr, bool &stop) {
     const int d = s.i & 15;
     const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
     uint32_t r0 = s.c0, r1 = s.c1;
@@ -456,7 +457,7 @@ __device__ __forceinline__ bool refine_try(const WarpCtx &w, const Row &row, con
         if (r0 == r1) r1 = add565(r1, 0, 1, 0);
         if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
     }
-    pr = palette_f(r0, r1, p.decoder, w.T->lut255, w.D);
+    pr = palette_f(r0, r1, p.decoder, lut, w.D);
     const float e = block_error<4>(row, p.cw, pr, s.base_idx);
     const bool accept = e < s.best;
     if (accept) {

@@ -42,6 +42,9 @@ __device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_
     }
 }
 
+constexpr size_t kRefineLutBytes = 256 * sizeof(float);
+constexpr size_t kRefineSmem = kRefineLutBytes + kWarpsPerCta * sizeof(float) * kWarpFloatsLow;
+
 constexpr int kRefillBatch = 16;  // 4: 3% slower, 8: 0.4%, 12: as 16 (hard mixture, level 9)
 
 __device__ __forceinline__ V3 shfl3(V3 v, int src) {
@@ -65,10 +68,16 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
                                                               const RefineSlot *st, int64_t n,
                                                               unsigned long long *counter, const ImageDesc *images,
                                                               RefineMap map) {
+    // Shared memory: the u8 table (all refinement needs of the staged
+    // tables), then each warp's 32 float texel rows -- six CTAs per SM.
     extern __shared__ __align__(16) unsigned char smem[];
-    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
-    stage_tables(T, G);
-    WarpCtx w = warp_ctx<1>(smem, T, G, p.decoder);
+    float *lut = reinterpret_cast<float *>(smem);
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = G->s.lut255[i];
+    __syncthreads();
+    WarpCtx w{};
+    w.D = &G->dec[p.decoder];
+    w.in = reinterpret_cast<float *>(smem + kRefineLutBytes) + (threadIdx.x >> 5) * kWarpFloatsLow;
+    w.lane = threadIdx.x & 31;
     const int lane = w.lane;
     float *row = w.in + lane * kInStride;
     EncodeParams lp = p;
@@ -113,17 +122,17 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
                             lp.three_color_black = di.three_color_black;
                             lp.cw = v3(di.cw[0], di.cw[1], di.cw[2]);
                             w.D = &G->dec[di.decoder];
-                            load_image_block(di, b, row, T.lut255);
+                            load_image_block(di, b, row, lut);
                             o = di.out + b;
                             er = di.errors ? di.errors + b : nullptr;
                         } else {
-                            if (MODE == 1) load_image_block(d, mine, row, T.lut255);
+                            if (MODE == 1) load_image_block(d, mine, row, lut);
                             else load_float_block_lane(s, mine, row);
                             o = out + mine;
                             er = errors ? errors + mine : nullptr;
                         }
                         const uint2 cur = *o;
-                        refine_begin(w, FloatRow{row}, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
+                        refine_begin(w, lut, FloatRow{row}, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
                         have = true;
                     }
                 }
@@ -134,7 +143,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
         bool accepted = false, stop = false;
         if (have) {
             PalF pr;
-            accepted = refine_try(w, FloatRow{row}, lp, r, pr, stop);
+            accepted = refine_try(w, lut, FloatRow{row}, lp, r, pr, stop);
             if (accepted) {
                 q0 = pr.c[0] * lp.cw;
                 q1 = pr.c[1] * lp.cw;
@@ -223,7 +232,7 @@ static cudaError_t refine_grid(int64_t n, int sms, size_t smem, int *grid) {
 cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
                           const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,
                           unsigned long long *counter, cudaStream_t stream, int sms) {
-    const size_t smem = smem_bytes(false);
+    const size_t smem = kRefineSmem;
     const ImageDesc dd = image ? *image : ImageDesc{};
     const BlocksSrc ss = blocks ? *blocks : BlocksSrc{nullptr, nullptr};
     const RefineMap none{nullptr, nullptr, 0};
@@ -240,7 +249,7 @@ cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const B
 cudaError_t launch_refine_batch(const GlobalTables *G, const ImageDesc *images, RefineMap map,
                                 const RefineSlot *slots, int64_t total, unsigned long long *counter,
                                 cudaStream_t stream, int sms) {
-    const size_t smem = smem_bytes(false);
+    const size_t smem = kRefineSmem;
     int grid = 0;
     cudaError_t e = refine_grid<2>(total, sms, smem, &grid);
     if (e != cudaSuccess) return e;
