@@ -394,6 +394,36 @@ def test_two_pass_batch_edge_cases(gpu_lib):
         assert same_bits(err.cpu().numpy(), oe), (c["img"].shape, c["level"])
 
 
+def test_batch_with_weight_plane_image(gpu_lib):
+    """A batch holding an image with a float weight plane runs the all-levels
+    float-row kernel in one pass (no lists); its images at every level, the
+    plane image included, equal the plain launches, blocks and errors."""
+    import torch
+    ig = gpu_lib
+    rng = np.random.default_rng(41)
+    w, h = 67, 45
+    plane = torch.from_numpy((rng.random((h, w)) * 2).astype(np.float32)).cuda()
+    imgs = [synth.quality_sweep_image(w, h, seed=70 + i) for i in range(10)]
+    devs = [_to_dev(im) for im in imgs]
+    nb = ig.blocks_of(w, h)
+    outs = [torch.zeros((nb, 8), dtype=torch.uint8, device="cuda") for _ in imgs]
+    errs = [torch.zeros(nb, dtype=torch.float32, device="cuda") for _ in imgs]
+    descs, plain = [], []
+    for i, (dev, out, err) in enumerate(zip(devs, outs, errs)):
+        wm, wp = (ig.WEIGHTS_PLANE, plane) if i == 4 else (ig.WEIGHTS_ALPHA, None)
+        descs.append(ig.image_desc(dev, i, out, err, i % 4, (0.299, 0.587, 0.114), wm, wp))
+        pe = torch.zeros(nb, dtype=torch.float32, device="cuda")
+        po = ig.compress_image(dev, i, i % 4, (0.299, 0.587, 0.114), wm, wp, errors=pe)
+        plain.append((po.cpu().numpy(), pe.cpu().numpy()))
+    batch = ig.Batch(descs)
+    batch.launch()
+    torch.cuda.synchronize()
+    for i, (out, err, (po, pe)) in enumerate(zip(outs, errs, plain)):
+        assert np.array_equal(out.cpu().numpy(), po), i
+        assert same_bits(err.cpu().numpy(), pe), i
+    batch.close()
+
+
 def test_decode_evaluate_golden(gpu_lib):
     import torch
     ig = gpu_lib
