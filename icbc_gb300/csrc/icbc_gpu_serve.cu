@@ -7,9 +7,11 @@
 // max_inflight streams -- so requests that arrive while a batch runs are
 // admitted as arena space frees up and their batch overlaps the running one
 // (copies on one stream run under another stream's kernel).  Each launch
-// copies its blocks to pinned staging; a host callback marks the launch done
-// and the scheduler hands the blocks to the callers' buffers and frees the
-// space.  No waits on the device side: the kernel drains a finite queue.
+// copies its blocks to pinned staging; a host callback marks the launch done,
+// the scheduler frees its device space and slot, and a delivery thread hands
+// the blocks to the callers' buffers (host copies off the scheduler's path)
+// and frees the staging.  No waits on the device side: the kernel drains a
+// finite queue.
 // A launch runs in the batched form's two passes: the blocks of 0 or 1
 // reduced colours of level-2..9 requests are finished by a register-only
 // pass, which lists the others in the request's own arena space.
@@ -25,6 +27,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/icbc_gpu.h"
@@ -139,6 +142,11 @@ struct icbc_gpu_server {
     std::mutex m;
     std::condition_variable cv_work, cv_done;
     std::deque<Request *> pending, admitted;
+    // Finished launches (requests, status) waiting for their host copies.
+    std::deque<std::pair<std::vector<Request *>, int>> delivery;
+    std::condition_variable cv_deliver;
+    std::thread deliverer;
+    bool scheduler_done = false;
     std::unordered_map<uint64_t, Request *> live;
     std::unordered_map<uint64_t, int> finished;
     std::vector<double> latencies;
@@ -249,14 +257,42 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
     return slot.status;
 }
 
-// Hands finished slots' blocks to the callers and frees their space.
-// Lock held on entry and exit; released around the host copies.
-void reap(icbc_gpu_server *S, std::unique_lock<std::mutex> &lock) {
+// Frees the slots whose launches finished and their requests' device and
+// input staging space (the GPU is done with them), and queues the requests
+// for delivery.  Lock held.
+void reap(icbc_gpu_server *S) {
     for (Slot &slot : S->slots) {
         if (!slot.busy || !slot.done.load(std::memory_order_acquire)) continue;
         std::vector<Request *> reqs;
         reqs.swap(slot.reqs);
-        const int status = slot.status;
+        for (Request *q : reqs) {
+            S->dev.release(q->dev_off, q->dev_bytes);
+            if (q->staged) S->in.release(q->in_off, q->in_bytes);
+        }
+        S->delivery.emplace_back(std::move(reqs), slot.status);
+        slot.busy = false;
+        slot.status = ICBC_GPU_OK;
+        slot.done.store(false, std::memory_order_relaxed);
+        S->in_flight--;
+        S->cv_deliver.notify_one();
+    }
+}
+
+// The delivery thread: copies each finished request's blocks (and errors)
+// from pinned staging to the caller's buffers, then frees the staging and
+// records the request as done.  Runs until the scheduler has stopped and
+// everything is delivered.
+void deliver(icbc_gpu_server *S) {
+    std::unique_lock<std::mutex> lock(S->m);
+    for (;;) {
+        if (S->delivery.empty()) {
+            if (S->scheduler_done) break;
+            S->cv_deliver.wait(lock);
+            continue;
+        }
+        std::vector<Request *> reqs = std::move(S->delivery.front().first);
+        const int status = S->delivery.front().second;
+        S->delivery.pop_front();
         lock.unlock();
         if (status == ICBC_GPU_OK) {
             for (Request *q : reqs) {
@@ -269,9 +305,7 @@ void reap(icbc_gpu_server *S, std::unique_lock<std::mutex> &lock) {
         const double t = now_ms();
         lock.lock();
         for (Request *q : reqs) {
-            S->dev.release(q->dev_off, q->dev_bytes);
             S->host.release(q->host_off, q->host_bytes);
-            if (q->staged) S->in.release(q->in_off, q->in_bytes);
             S->live.erase(q->id);
             S->finished[q->id] = status;
             if (status == ICBC_GPU_OK) {
@@ -283,11 +317,8 @@ void reap(icbc_gpu_server *S, std::unique_lock<std::mutex> &lock) {
             }
             delete q;
         }
-        slot.busy = false;
-        slot.status = ICBC_GPU_OK;
-        slot.done.store(false, std::memory_order_relaxed);
-        S->in_flight--;
         S->cv_done.notify_all();
+        S->cv_work.notify_one();  // staging space freed: admission may go on
     }
 }
 
@@ -295,7 +326,7 @@ void scheduler(icbc_gpu_server *S) {
     cudaSetDevice(S->device);
     std::unique_lock<std::mutex> lock(S->m);
     for (;;) {
-        reap(S, lock);
+        reap(S);
         // Admission, first come first served: stop at the first request that
         // does not fit, so a large one is not starved by small ones.
         while (!S->pending.empty()) {
@@ -331,6 +362,8 @@ void scheduler(icbc_gpu_server *S) {
         if (S->stop && S->admitted.empty() && S->in_flight == 0) break;
         S->cv_work.wait_for(lock, std::chrono::microseconds(100));
     }
+    S->scheduler_done = true;
+    S->cv_deliver.notify_all();
 }
 
 }  // namespace
@@ -387,6 +420,7 @@ int icbc_gpu_server_create(const icbc_gpu_server_config *config, icbc_gpu_server
     S->host.reset(stage);
     S->in.reset(in_stage);
     S->worker = std::thread(scheduler, S);
+    S->deliverer = std::thread(deliver, S);
     *server = S;
     return ICBC_GPU_OK;
 }
@@ -539,6 +573,7 @@ int icbc_gpu_server_destroy(icbc_gpu_server *S) {
         S->cv_work.notify_all();
     }
     if (S->worker.joinable()) S->worker.join();
+    if (S->deliverer.joinable()) S->deliverer.join();
     for (Slot &slot : S->slots) {
         if (slot.stream) cudaStreamSynchronize(slot.stream);
         if (slot.stream) cudaStreamDestroy(slot.stream);
