@@ -100,7 +100,8 @@ struct Request {
     int64_t dpitch = 0;
     size_t dev_off = 0, dev_bytes = 0, out_off = 0, err_off = 0, list_off = 0;
     size_t host_off = 0, host_bytes = 0;
-    size_t in_off = 0, in_bytes = 0;  // pinned copy of the texels (rows at dpitch)
+    size_t in_off = 0, in_bytes = 0;  // pinned copy of the texels (rows at dpitch), then at levels 4-9 the
+                                      // zero blocks the encoder starts from, laid out as on the device
     bool staged = false;
     double t_submit = 0.0;
 };
@@ -201,12 +202,12 @@ int launch_slot(icbc_gpu_server *S, Slot &slot) {
         d.out = reinterpret_cast<uint2 *>(base + q->out_off);
         d.errors = q->r.errors ? reinterpret_cast<float *>(base + q->err_off) : nullptr;
         if (q->staged)
-            e = cudaMemcpyAsync(base, S->h_in + q->in_off, (size_t)q->dpitch * q->r.height, cudaMemcpyHostToDevice,
-                                slot.stream);
+            e = cudaMemcpyAsync(base, S->h_in + q->in_off, q->in_bytes, cudaMemcpyHostToDevice, slot.stream);
         else
             e = cudaMemcpy2DAsync(base, (size_t)q->dpitch, q->r.rgba, (size_t)q->r.pitch, 4 * (size_t)q->r.width,
                                   (size_t)q->r.height, cudaMemcpyHostToDevice, slot.stream);
-        if (e == cudaSuccess && d.level >= 4) e = cudaMemsetAsync(d.out, 0, (size_t)d.nblocks * 8, slot.stream);
+        if (e == cudaSuccess && d.level >= 4 && !q->staged)
+            e = cudaMemsetAsync(d.out, 0, (size_t)d.nblocks * 8, slot.stream);
         slot.h_images[i] = d;
         slot.h_start[i] = total;
         slot.h_list_base[i] = d.level >= 2 && d.nblocks > 0 ? (int64_t)((q->dev_off + q->list_off) / 4) : -1;
@@ -466,7 +467,11 @@ int icbc_gpu_server_submit(icbc_gpu_server *S, const icbc_gpu_request *req, uint
         delete q;
         return ICBC_GPU_ERR_CANCELLED;
     }
-    q->in_bytes = (size_t)q->dpitch * req->height;
+    // Levels 4-9 start from zero blocks (the kernels keep prior bytes where
+    // no candidate is finite): staged, they travel with the texels in one
+    // copy; otherwise the launch clears them.
+    const size_t zero_blocks = req->level >= 4 ? (size_t)q->d.nblocks * 8 : 0;
+    q->in_bytes = zero_blocks ? q->out_off + zero_blocks : (size_t)q->dpitch * req->height;
     q->staged = S->in.alloc(q->in_bytes, &q->in_off);
     if (q->staged) {
         // The region belongs to this request now: fill it without the lock.
@@ -474,6 +479,7 @@ int icbc_gpu_server_submit(icbc_gpu_server *S, const icbc_gpu_request *req, uint
         const size_t row = 4 * (size_t)req->width;
         for (int32_t y = 0; y < req->height; y++)
             std::memcpy(S->h_in + q->in_off + (size_t)y * q->dpitch, req->rgba + (size_t)y * req->pitch, row);
+        if (zero_blocks) std::memset(S->h_in + q->in_off + q->out_off, 0, zero_blocks);
         lock.lock();
     }
     q->id = S->next_id++;
