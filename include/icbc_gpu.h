@@ -253,7 +253,8 @@ typedef struct icbc_gpu_server_stats {
 } icbc_gpu_server_stats;
 
 /* Creates the server on the current device: allocates the arena and pinned
- * staging, starts the scheduler thread. */
+ * staging, starts the scheduler thread (admission, launches) and the
+ * delivery thread (finished blocks into the callers' buffers). */
 int icbc_gpu_server_create(const icbc_gpu_server_config *config, icbc_gpu_server **server);
 /* Queues a request; returns its id.  The texels are copied to pinned staging
  * on the calling thread when there is room (else at launch, from `rgba`).
