@@ -28,6 +28,8 @@ DECODER_DEFAULT = -1
 Quality_Fast, Quality_Default, Quality_Max = 1, 8, 9
 # weight sources of RGBA8 images
 WEIGHTS_UNIFORM, WEIGHTS_ALPHA, WEIGHTS_PLANE = 0, 1, 2
+# largest batch of icbc_gpu_compress_bc1_images_noalloc (ICBC_GPU_NOALLOC_MAX_IMAGES)
+NOALLOC_MAX_IMAGES = 256
 # SIMD builds of the reference whose output the *_simd entry points reproduce.
 SIMD_SCALAR, SIMD_SSE2, SIMD_SSE41, SIMD_AVX, SIMD_AVX2, SIMD_AVX512 = 0, 1, 2, 3, 4, 5
 
@@ -402,6 +404,32 @@ def evaluate_errors(rgba_blocks, blocks, decoder: int = Decoder_D3D10, stream=No
         out = torch.empty(n, dtype=torch.float32, device=blocks.device)
         _check(load().icbc_gpu_evaluate_bc1_error(r.data_ptr(), b.data_ptr(), out.data_ptr(), n, int(decoder),
                                                   _stream_ptr(stream)), "evaluate_bc1_error")
+    return out
+
+
+def decode_bc3_blocks(blocks, decoder: int = Decoder_D3D10, stream=None):
+    """decode_bc3 (as the reference implements it) over a CUDA uint8 tensor
+    (n,16) -> (n,64) RGBA8."""
+    torch = _torch()
+    n = blocks.shape[0]
+    with _on(stream):
+        b = blocks.contiguous()
+        out = torch.empty((n, 64), dtype=torch.uint8, device=blocks.device)
+        _check(load().icbc_gpu_decode_bc3(b.data_ptr(), out.data_ptr(), n, int(decoder), _stream_ptr(stream)),
+               "decode_bc3")
+    return out
+
+
+def evaluate_bc3_errors(rgba_blocks, blocks, alpha_blend: bool, decoder: int = Decoder_D3D10, stream=None):
+    """evaluate_bc3_error over CUDA tensors (n,64) uint8 and (n,16) uint8 -> (n,) float32."""
+    torch = _torch()
+    n = blocks.shape[0]
+    with _on(stream):
+        r, b = rgba_blocks.contiguous(), blocks.contiguous()
+        out = torch.empty(n, dtype=torch.float32, device=blocks.device)
+        _check(load().icbc_gpu_evaluate_bc3_error(r.data_ptr(), b.data_ptr(), out.data_ptr(), n,
+                                                  int(bool(alpha_blend)), int(decoder), _stream_ptr(stream)),
+               "evaluate_bc3_error")
     return out
 
 

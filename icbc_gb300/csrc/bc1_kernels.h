@@ -131,6 +131,9 @@ inline int batch_ctas_per_sm(bool byte_rows = false) {
 cudaError_t launch_decode(const void *blocks, void *rgba, int64_t n, int decoder, cudaStream_t stream);
 cudaError_t launch_evaluate(const void *rgba, const void *blocks, float *errors, int64_t n, int decoder,
                             cudaStream_t stream);
+cudaError_t launch_decode_bc3(const void *blocks, void *rgba, int64_t n, int decoder, cudaStream_t stream);
+cudaError_t launch_evaluate_bc3(const void *rgba, const void *blocks, float *errors, int64_t n, int alpha_blend,
+                                int decoder, cudaStream_t stream);
 
 // Level-9 refinement pass (bc1_refine.cu) and its stream-ordered scratch.
 cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream);

@@ -21,7 +21,7 @@ struct ThreadState {
     cudaStream_t stream = nullptr;
     float *d_colors = nullptr;   // 64 floats
     float *d_weights = nullptr;  // 16 floats
-    uint8_t *d_block = nullptr;  // 8 bytes
+    uint8_t *d_block = nullptr;  // 16 bytes (a BC1 or BC3 block)
     float *d_error = nullptr;
     uint8_t *d_rgba = nullptr;   // 64 bytes
     bool ok = false;
@@ -98,5 +98,34 @@ float evaluate_bc1_error(const unsigned char rgba_block[16 * 4], const void *blo
     if (e == cudaSuccess) e = cudaStreamSynchronize(T.stream);
     return e == cudaSuccess ? error : NAN;
 }
+
+void decode_bc3(const void *block, unsigned char rgba_block[16 * 4], Decoder decoder) {
+    ThreadState &T = t_state;
+    if (!T.ready()) return;
+    if (cudaMemcpyAsync(T.d_block, block, 16, cudaMemcpyHostToDevice, T.stream) != cudaSuccess) return;
+    if (icbc_gpu_decode_bc3(T.d_block, T.d_rgba, 1, (int)decoder, T.stream) != ICBC_GPU_OK) return;
+    if (cudaMemcpyAsync(rgba_block, T.d_rgba, 64, cudaMemcpyDeviceToHost, T.stream) != cudaSuccess) return;
+    cudaStreamSynchronize(T.stream);
+}
+
+float evaluate_bc3_error(const unsigned char rgba_block[16 * 4], const void *block, bool alpha_blend,
+                         Decoder decoder) {
+    ThreadState &T = t_state;
+    if (!T.ready()) return NAN;
+    cudaError_t e = cudaMemcpyAsync(T.d_block, block, 16, cudaMemcpyHostToDevice, T.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T.d_rgba, rgba_block, 64, cudaMemcpyHostToDevice, T.stream);
+    if (e != cudaSuccess) return NAN;
+    if (icbc_gpu_evaluate_bc3_error(T.d_rgba, T.d_block, T.d_error, 1, alpha_blend, (int)decoder, T.stream) !=
+        ICBC_GPU_OK)
+        return NAN;
+    float error = NAN;
+    e = cudaMemcpyAsync(&error, T.d_error, sizeof(float), cudaMemcpyDeviceToHost, T.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(T.stream);
+    return e == cudaSuccess ? error : NAN;
+}
+
+// The reference has no BC3 encoder: compress_bc3 returns 0 and leaves the
+// output untouched (icbc.h:3850-3853).
+float compress_bc3(Quality, const float *, const float *, const float *, bool, void *) { return 0.0f; }
 
 }  // namespace icbc

@@ -744,6 +744,32 @@ int icbc_gpu_evaluate_bc1_error(const uint8_t *d_rgba, const void *d_blocks, flo
     return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
 }
 
+int icbc_gpu_decode_bc3(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks, int decoder, void *stream) {
+    if (n_blocks < 0) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (n_blocks == 0) return ICBC_GPU_OK;
+    if (!d_blocks || !d_rgba) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(d_blocks, 16) || !aligned(d_rgba, 16)) return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(decoder, &dec);
+    if (st) return st;
+    cudaError_t e = launch_decode_bc3(d_blocks, d_rgba, n_blocks, dec, reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
+int icbc_gpu_evaluate_bc3_error(const uint8_t *d_rgba, const void *d_blocks, float *d_errors, int64_t n_blocks,
+                                int alpha_blend, int decoder, void *stream) {
+    if (n_blocks < 0) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (n_blocks == 0) return ICBC_GPU_OK;
+    if (!d_blocks || !d_rgba || !d_errors) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    if (!aligned(d_blocks, 16) || !aligned(d_rgba, 16) || !aligned(d_errors, 4)) return ICBC_GPU_ERR_MISALIGNED;
+    int dec = 0;
+    int st = resolve_decoder(decoder, &dec);
+    if (st) return st;
+    cudaError_t e = launch_evaluate_bc3(d_rgba, d_blocks, d_errors, n_blocks, alpha_blend != 0, dec,
+                                        reinterpret_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
+}
+
 // Device buffers of the host-buffer path, grown on demand and reused.
 namespace {
 // The host-buffer path works in bands of block rows: band i's texels go up

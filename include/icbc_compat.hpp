@@ -9,8 +9,10 @@
 //
 // Like icbc::init, init() selects the decoder compress_bc1 uses; it must not
 // run concurrently with compress_bc1.  The other functions are thread-safe.
-// BC3 (compress_bc3, decode_bc3, evaluate_bc3_error) is not provided: the
-// reference leaves it unimplemented (icbc.h:3850-3853).
+// BC3 behaves as the reference's does: decode_bc3 and evaluate_bc3_error use
+// the colour half's 4-colour palette and alpha0 for every texel (the
+// reference's alpha index is always 0, icbc.h:2929-2947, :3048-3071), and
+// compress_bc3 returns 0 without writing the block (icbc.h:3850-3853).
 #ifndef ICBC_COMPAT_HPP
 #define ICBC_COMPAT_HPP
 
@@ -43,11 +45,16 @@ enum Quality {
 };
 
 void decode_bc1(const void *block, unsigned char rgba_block[16 * 4], Decoder decoder = Decoder_D3D10);
+void decode_bc3(const void *block, unsigned char rgba_block[16 * 4], Decoder decoder = Decoder_D3D10);
 
 float evaluate_bc1_error(const unsigned char rgba_block[16 * 4], const void *block, Decoder decoder = Decoder_D3D10);
+float evaluate_bc3_error(const unsigned char rgba_block[16 * 4], const void *block, bool alpha_blend,
+                         Decoder decoder = Decoder_D3D10);
 
 float compress_bc1(Quality level, const float *input_colors, const float *input_weights, const float color_weights[3],
                    bool three_color_mode, bool three_color_black, void *output);
+float compress_bc3(Quality level, const float *input_colors, const float *input_weights, const float color_weights[3],
+                   bool six_alpha_mode, void *output);
 
 }  // namespace icbc
 

@@ -202,6 +202,19 @@ int icbc_gpu_decode_bc1(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks,
 int icbc_gpu_evaluate_bc1_error(const uint8_t *d_rgba, const void *d_blocks, float *d_errors,
                                 int64_t n_blocks, int decoder, void *stream);
 
+/* BC3 as the reference implements it (its BC3 encoder is not written:
+ * icbc::compress_bc3 returns 0 without touching the block, icbc.h:3850-3853).
+ * A 16-byte block is a BC4 alpha half (alpha0, alpha1, 6 index bytes) then a
+ * BC1 block.  Decoding uses the colour block's 4-colour palette whatever the
+ * endpoint order, and the reference's alpha index is always 0, so every texel
+ * gets alpha0.  Replace icbc::decode_bc3 (icbc.h:39, :2929-2947) and
+ * icbc::evaluate_bc3_error (icbc.h:44, :3048-3071): per texel, the squared
+ * colour error (times alpha / 255 when alpha_blend) plus the squared alpha0
+ * difference.  Blocks 16-byte aligned. */
+int icbc_gpu_decode_bc3(const void *d_blocks, uint8_t *d_rgba, int64_t n_blocks, int decoder, void *stream);
+int icbc_gpu_evaluate_bc3_error(const uint8_t *d_rgba, const void *d_blocks, float *d_errors, int64_t n_blocks,
+                                int alpha_blend, int decoder, void *stream);
+
 /* End-to-end call with HOST buffers: copies the image in, encodes, copies the
  * blocks (and errors if non-NULL) out, and returns when they are on the host.
  * rgba is host memory (pitch bytes per row), weight_plane host floats

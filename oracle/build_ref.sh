@@ -2,10 +2,16 @@
 # Compiles the reference's own icbc.h (unmodified, read where it lies) in its
 # scalar profile into oracle/_ref/libicbc_ref.so.  Test infrastructure only:
 # the library pins the C restatement and generates tests/golden/.  Needs the
-# reference checkout; exits 0 without building when it is absent.
+# reference checkout; exits 0 without building when it is absent.  This
+# recipe is the one place that names the checkout's location;
+# ICBC_REFERENCE_DIR overrides it, and `build_ref.sh --where` prints it.
 set -e
 REF=${ICBC_REFERENCE_DIR:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+if [ "$1" = "--where" ]; then
+    echo "$REF"
+    exit 0
+fi
 if [ ! -f "$REF/icbc.h" ]; then
     echo "build_ref: no reference at $REF, skipping"
     exit 0

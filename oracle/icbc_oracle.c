@@ -132,16 +132,15 @@ static c32 vector3_to_color32(v3 v) {
 
 /* ------------------------------------------------------------- palettes */
 
-/* Palette of a block for each hardware decoder (icbc.h:2751-2881).  The
- * 4-colour form is chosen when col0 > col1, else the 3-colour form with
- * palette[3] = 0. */
-static void eval_palette32(uint16_t u0, uint16_t u1, c32 p[4], int decoder) {
+/* Palette of a block for each hardware decoder (icbc.h:2751-2881): the
+ * 4-colour form when `four`, else the 3-colour form with palette[3] = 0. */
+static void eval_palette32_form(uint16_t u0, uint16_t u1, c32 p[4], int decoder, int four) {
     p[0] = expand565(u0);
     p[1] = expand565(u1);
     const int r0 = (u0 >> 11) & 31, b0 = u0 & 31, r1 = (u1 >> 11) & 31, b1 = u1 & 31;
     const c32 zero = {0, 0, 0, 0};
     if (decoder == ORACLE_D3D10) {                               /* :2752-2779 */
-        if (u0 > u1) {
+        if (four) {
             p[2].r = (2 * p[0].r + p[1].r) / 3; p[2].g = (2 * p[0].g + p[1].g) / 3;
             p[2].b = (2 * p[0].b + p[1].b) / 3; p[2].a = 255;
             p[3].r = (2 * p[1].r + p[0].r) / 3; p[3].g = (2 * p[1].g + p[0].g) / 3;
@@ -153,7 +152,7 @@ static void eval_palette32(uint16_t u0, uint16_t u1, c32 p[4], int decoder) {
         }
     } else if (decoder == ORACLE_NVIDIA) {                       /* :2782-2812 */
         int gdiff = p[1].g - p[0].g;
-        if (u0 > u1) {
+        if (four) {
             p[2].r = (((2 * r0 + r1) * 22) / 8) & 255;
             p[2].g = ((256 * p[0].g + gdiff / 4 + 128 + gdiff * 80) / 256) & 255;
             p[2].b = (((2 * b0 + b1) * 22) / 8) & 255;
@@ -170,7 +169,7 @@ static void eval_palette32(uint16_t u0, uint16_t u1, c32 p[4], int decoder) {
             p[3] = zero;
         }
     } else if (decoder == ORACLE_AMD) {                          /* :2815-2843 */
-        if (u0 > u1) {
+        if (four) {
             p[2].r = (43 * p[0].r + 21 * p[1].r + 32) >> 6; p[2].g = (43 * p[0].g + 21 * p[1].g + 32) >> 6;
             p[2].b = (43 * p[0].b + 21 * p[1].b + 32) >> 6; p[2].a = 255;
             p[3].r = (43 * p[1].r + 21 * p[0].r + 32) >> 6; p[3].g = (43 * p[1].g + 21 * p[0].g + 32) >> 6;
@@ -181,7 +180,7 @@ static void eval_palette32(uint16_t u0, uint16_t u1, c32 p[4], int decoder) {
             p[3] = zero;
         }
     } else {                                                     /* Intel :2846-2874 */
-        if (u0 > u1) {
+        if (four) {
             p[2].r = (171 * p[0].r + 85 * p[1].r + 128) >> 8; p[2].g = (171 * p[0].g + 85 * p[1].g + 128) >> 8;
             p[2].b = (171 * p[0].b + 85 * p[1].b + 128) >> 8; p[2].a = 255;
             p[3].r = (171 * p[1].r + 85 * p[0].r + 128) >> 8; p[3].g = (171 * p[1].g + 85 * p[0].g + 128) >> 8;
@@ -192,6 +191,11 @@ static void eval_palette32(uint16_t u0, uint16_t u1, c32 p[4], int decoder) {
             p[3] = zero;
         }
     }
+}
+
+/* evaluate_palette (icbc.h:2876-2881): the 4-colour form when col0 > col1. */
+static void eval_palette32(uint16_t u0, uint16_t u1, c32 p[4], int decoder) {
+    eval_palette32_form(u0, u1, p, decoder, u0 > u1);
 }
 
 /* Float palette (icbc.h:2893-2900). */
@@ -965,6 +969,44 @@ float oracle_evaluate_bc1_error(const uint8_t rgba[64], const void *block, int d
     for (int i = 0; i < 16; i++) {
         c32 c = {rgba[4 * i + 0], rgba[4 * i + 1], rgba[4 * i + 2], 255};
         error += (float)c32_mse(pal[(b.indices >> (2 * i)) & 3], c);
+    }
+    return error;
+}
+
+/* icbc::decode_bc3 (icbc.h:2929-2947, :3824-3826): BlockBC3 is the BC4
+ * alpha half (alpha0, alpha1, 6 index bytes) then a BC1 block.  The colour
+ * palette is always the 4-colour form (evaluate_palette4, icbc.h:2882-2891).
+ * The reference's alpha palette only sets entries 0 and 1 and its alpha index
+ * is always 0, so every texel's alpha is alpha0. */
+void oracle_decode_bc3(const void *block, uint8_t rgba[64], int decoder) {
+    const uint8_t *q = (const uint8_t *)block;
+    blk b;
+    load_block(q + 8, &b);
+    c32 pal[4];
+    eval_palette32_form(b.col0, b.col1, pal, decoder & 3, 1);
+    for (int i = 0; i < 16; i++) {
+        c32 c = pal[(b.indices >> (2 * i)) & 3];
+        rgba[4 * i + 0] = (uint8_t)c.r; rgba[4 * i + 1] = (uint8_t)c.g;
+        rgba[4 * i + 2] = (uint8_t)c.b; rgba[4 * i + 3] = q[0];
+    }
+}
+
+/* icbc::evaluate_bc3_error (icbc.h:3048-3071, :3841-3843): per texel, in
+ * order, the colour error scaled by alpha / 255 when alpha_blend, then the
+ * squared difference of alpha0 and the texel's alpha. */
+float oracle_evaluate_bc3_error(const uint8_t rgba[64], const void *block, int alpha_blend, int decoder) {
+    const uint8_t *q = (const uint8_t *)block;
+    blk b;
+    load_block(q + 8, &b);
+    c32 pal[4];
+    eval_palette32_form(b.col0, b.col1, pal, decoder & 3, 1);
+    float error = 0.0f;
+    for (int i = 0; i < 16; i++) {
+        c32 c = {rgba[4 * i + 0], rgba[4 * i + 1], rgba[4 * i + 2], rgba[4 * i + 3]};
+        const float scale = alpha_blend ? ((float)c.a * 1.0f) / 255.0f : 1.0f;
+        error += scale * (float)c32_mse(pal[(b.indices >> (2 * i)) & 3], c);
+        const int da = (int)q[0] - (int)c.a;
+        error += (float)(da * da);
     }
     return error;
 }

@@ -99,6 +99,12 @@ void oracle_fetch_block(const uint8_t *rgba, int w, int h, int64_t pitch_bytes,
 void oracle_decode_bc1(const void *block, uint8_t rgba[64], int decoder);
 float oracle_evaluate_bc1_error(const uint8_t rgba[64], const void *block, int decoder);
 
+/* icbc::decode_bc3 (icbc.h:39, :2929-2947) and icbc::evaluate_bc3_error
+ * (icbc.h:44, :3048-3071) as the reference implements them: 16-byte blocks,
+ * 4-colour palette, alpha0 for every texel. */
+void oracle_decode_bc3(const void *block, uint8_t rgba[64], int decoder);
+float oracle_evaluate_bc3_error(const uint8_t rgba[64], const void *block, int alpha_blend, int decoder);
+
 /* FP64 decode-and-compare of a whole image: sum of squared RGB differences
  * over every texel of every (edge-replicated) block.  Returns the sum; mse
  * per texel = sum / (16 * blocks). */

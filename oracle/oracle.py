@@ -65,6 +65,14 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+def reference_dir() -> str | None:
+    """Where build_ref.sh finds the reference checkout (it holds the default;
+    ICBC_REFERENCE_DIR overrides it), or None where there is none."""
+    r = subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), "--where"], capture_output=True, text=True)
+    path = r.stdout.strip()
+    return path if r.returncode == 0 and path and os.path.exists(os.path.join(path, "icbc.h")) else None
+
+
 def build_ref() -> str | None:
     """Builds oracle/_ref/libicbc_ref.so when the reference checkout exists."""
     script = os.path.join(HERE, "build_ref.sh")
@@ -102,6 +110,10 @@ def lib():
             L.oracle_decode_bc1.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
             L.oracle_evaluate_bc1_error.restype = ctypes.c_float
             L.oracle_evaluate_bc1_error.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+            L.oracle_decode_bc3.restype = None
+            L.oracle_decode_bc3.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+            L.oracle_evaluate_bc3_error.restype = ctypes.c_float
+            L.oracle_evaluate_bc3_error.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
             L.oracle_image_sse.restype = ctypes.c_double
             L.oracle_image_sse.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
                                            ctypes.c_void_p, ctypes.c_int]
@@ -138,6 +150,11 @@ def ref(profile: int = 0):
             R.ref_decode_bc1.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
             R.ref_evaluate_bc1_error.restype = ctypes.c_float
             R.ref_evaluate_bc1_error.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+            if profile == 0:
+                R.ref_decode_bc3.restype = None
+                R.ref_decode_bc3.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+                R.ref_evaluate_bc3_error.restype = ctypes.c_float
+                R.ref_evaluate_bc3_error.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
             _ref[profile] = R
     return _ref[profile]
 
@@ -241,6 +258,24 @@ def evaluate_bc1_error(rgba_blocks, blocks, decoder=0):
                      for i in range(b.shape[0])], np.float32)
 
 
+def decode_bc3(blocks, decoder=0):
+    """icbc::decode_bc3 of 16-byte blocks -> (n, 64) RGBA8."""
+    L = lib()
+    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 16)
+    out = np.zeros((b.shape[0], 64), np.uint8)
+    for i in range(b.shape[0]):
+        L.oracle_decode_bc3(b[i].ctypes.data, out[i].ctypes.data, int(decoder))
+    return out
+
+
+def evaluate_bc3_error(rgba_blocks, blocks, alpha_blend, decoder=0):
+    L = lib()
+    t = np.ascontiguousarray(rgba_blocks, dtype=np.uint8).reshape(-1, 64)
+    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 16)
+    return np.array([L.oracle_evaluate_bc3_error(t[i].ctypes.data, b[i].ctypes.data, int(bool(alpha_blend)),
+                                                 int(decoder)) for i in range(b.shape[0])], np.float32)
+
+
 def image_sse(rgba, blocks, decoder=0):
     L = lib()
     rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
@@ -307,6 +342,27 @@ def ref_evaluate_bc1_error(rgba_blocks, blocks, decoder=0):
     b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 8)
     return np.array([R.ref_evaluate_bc1_error(t[i].ctypes.data, b[i].ctypes.data, int(decoder))
                      for i in range(b.shape[0])], np.float32)
+
+
+def ref_decode_bc3(blocks, decoder=0):
+    R = ref()
+    if R is None:
+        return None
+    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 16)
+    out = np.zeros((b.shape[0], 64), np.uint8)
+    for i in range(b.shape[0]):
+        R.ref_decode_bc3(b[i].ctypes.data, out[i].ctypes.data, int(decoder))
+    return out
+
+
+def ref_evaluate_bc3_error(rgba_blocks, blocks, alpha_blend, decoder=0):
+    R = ref()
+    if R is None:
+        return None
+    t = np.ascontiguousarray(rgba_blocks, dtype=np.uint8).reshape(-1, 64)
+    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 16)
+    return np.array([R.ref_evaluate_bc3_error(t[i].ctypes.data, b[i].ctypes.data, int(bool(alpha_blend)),
+                                              int(decoder)) for i in range(b.shape[0])], np.float32)
 
 
 def expand_rgba8(pixels):

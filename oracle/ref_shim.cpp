@@ -37,4 +37,14 @@ float ref_evaluate_bc1_error(const unsigned char *rgba, const void *block, int d
     return icbc::evaluate_bc1_error(rgba, block, (icbc::Decoder)decoder);
 }
 
+// icbc::decode_bc3 (icbc.h:39, :3824-3826).
+void ref_decode_bc3(const void *block, unsigned char *rgba, int decoder) {
+    icbc::decode_bc3(block, rgba, (icbc::Decoder)decoder);
+}
+
+// icbc::evaluate_bc3_error (icbc.h:44, :3841-3843).
+float ref_evaluate_bc3_error(const unsigned char *rgba, const void *block, int alpha_blend, int decoder) {
+    return icbc::evaluate_bc3_error(rgba, block, alpha_blend != 0, (icbc::Decoder)decoder);
+}
+
 }

@@ -5,7 +5,11 @@
 // input:  int32 n, decoder, nlevels, levels[nlevels], float cw[3],
 //         n x (64 floats colors, 16 floats weights, 64 bytes rgba)
 // output: per level, n x (8 bytes block, float error); then for the last
-//         level n x (64 bytes decoded, float evaluate_bc1_error)
+//         level n x (64 bytes decoded, float evaluate_bc1_error); then per
+//         block the 16-byte BC3 block {alpha0 = i, alpha1 = 255 - i, 6 index
+//         bytes = i, the BC1 block} x (64 bytes decode_bc3, float
+//         evaluate_bc3_error with alpha_blend, float compress_bc3's return,
+//         1 byte: compress_bc3 left the block as it was)
 #include <cstdio>
 #include <cstdint>
 #include <vector>
@@ -48,6 +52,23 @@ int main(int argc, char **argv) {
         float e = icbc::evaluate_bc1_error(&rgba[64 * i], &blocks[8 * i], (icbc::Decoder)decoder);
         std::fwrite(dec, 1, 64, o);
         std::fwrite(&e, 4, 1, o);
+    }
+    for (int i = 0; i < n; i++) {
+        unsigned char bc3[16], before[16], dec[64];
+        bc3[0] = (unsigned char)i;
+        bc3[1] = (unsigned char)(255 - i);
+        for (int k = 2; k < 8; k++) bc3[k] = (unsigned char)i;
+        for (int k = 0; k < 8; k++) bc3[8 + k] = blocks[8 * i + k];
+        icbc::decode_bc3(bc3, dec, (icbc::Decoder)decoder);
+        float e = icbc::evaluate_bc3_error(&rgba[64 * i], bc3, true, (icbc::Decoder)decoder);
+        for (int k = 0; k < 16; k++) before[k] = bc3[k];
+        float c = icbc::compress_bc3(icbc::Quality_Default, &colors[64 * i], &weights[16 * i], cw, false, bc3);
+        unsigned char same = 1;
+        for (int k = 0; k < 16; k++) same &= (unsigned char)(before[k] == bc3[k]);
+        std::fwrite(dec, 1, 64, o);
+        std::fwrite(&e, 4, 1, o);
+        std::fwrite(&c, 4, 1, o);
+        std::fwrite(&same, 1, 1, o);
     }
     std::fclose(o);
     return 0;

@@ -13,6 +13,10 @@ stores inputs and outputs:
                three-colour flags on; plus the SHA-256 of the generated image
   decode.npz   decode_bc1 and evaluate_bc1_error of the reference for every
                decoder on encoded blocks, including 3-colour blocks
+  bc3.npz      decode_bc3 and evaluate_bc3_error (alpha_blend off and on)
+               of the reference for every decoder on 16-byte blocks whose
+               colour halves are encoded blocks (both endpoint orders) and
+               whose alpha halves are random bytes
   simd.npz     the reference's x86 SIMD builds (ICBC_SIMD 1..5, compiled
                without FP contraction by the same script) on two sets of 128
                image blocks -- the blocks of two 512x512 images where some
@@ -20,7 +24,7 @@ stores inputs and outputs:
                first others -- at levels 2, 4, 8, 9 x decoder x
                (three_color_mode, three_color_black) in {(1, 1), (0, 0)}
 
-Usage: python tests/golden/make_golden.py [simd]   (simd: only simd.npz)
+Usage: python tests/golden/make_golden.py [simd|bc3]   (only simd.npz / bc3.npz)
 """
 from __future__ import annotations
 
@@ -116,11 +120,33 @@ def golden_simd():
     print("simd.npz", os.path.getsize(os.path.join(HERE, "simd.npz")))
 
 
+def golden_bc3(blocks, rgba):
+    """BC3 decode/evaluate of the reference on `blocks` (n, 8) colour halves
+    with random alpha halves, against `rgba` (n, 64) with random alpha."""
+    n = blocks.shape[0]
+    r = synth.randint(77, 0, (n, 8), 0, 256).astype(np.uint8)
+    bc3 = np.concatenate([r, blocks], axis=1)
+    tex = rgba.copy().reshape(n, 16, 4)
+    tex[:, :, 3] = synth.randint(77, 1, (n, 16), 0, 256).astype(np.uint8)
+    tex = tex.reshape(n, 64)
+    out = {"blocks": bc3, "rgba": tex}
+    for d in range(4):
+        out["decoded_D%d" % d] = O.ref_decode_bc3(bc3, d)
+        for ab in (0, 1):
+            out["error_D%d_blend%d" % (d, ab)] = O.ref_evaluate_bc3_error(tex, bc3, ab, d)
+    np.savez_compressed(os.path.join(HERE, "bc3.npz"), **out)
+    print("bc3.npz", os.path.getsize(os.path.join(HERE, "bc3.npz")))
+
+
 def main():
     if O.ref() is None:
         raise SystemExit("the reference checkout is needed to generate golden vectors")
     if sys.argv[1:] == ["simd"]:
         golden_simd()
+        return
+    if sys.argv[1:] == ["bc3"]:
+        g = np.load(os.path.join(HERE, "decode.npz"))
+        golden_bc3(g["blocks"], g["rgba"])
         return
     colors, wr = golden_blocks()
     n = colors.shape[0]
@@ -159,6 +185,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "decode.npz"), **dec_out)
     for f in ("blocks.npz", "image512.npz", "decode.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
+    golden_bc3(blocks, rgba2)
     golden_simd()
 
 

@@ -14,14 +14,14 @@ from icbc_gb300 import synth
 from oracle import oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_HEADER_DIR = os.environ.get("ICBC_REFERENCE_DIR", "/root/reference")
+REF_HEADER_DIR = O.reference_dir()
 
 
 def _cxx():
     return shutil.which(os.environ.get("CXX", "g++"))
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF_HEADER_DIR, "icbc.h")) or not _cxx(),
+@pytest.mark.skipif(not REF_HEADER_DIR or not _cxx(),
                     reason="reference header or C++ compiler not available")
 def test_reference_header_symbols_resolve():
     """Every icbc:: symbol a caller compiled against the reference's icbc.h
@@ -34,8 +34,11 @@ def test_reference_header_symbols_resolve():
                     'float use(const float *c, const float *w, const float *cw, void *o, unsigned char *t) {\n'
                     '  icbc::init(icbc::Decoder_NVIDIA);\n'
                     '  icbc::decode_bc1(o, t);\n'
+                    '  icbc::decode_bc3(o, t, icbc::Decoder_Intel);\n'
                     '  return icbc::compress_bc1(icbc::Quality_Max, c, w, cw, true, true, o) +\n'
-                    '         icbc::evaluate_bc1_error(t, o, icbc::Decoder_AMD);\n}\n')
+                    '         icbc::evaluate_bc1_error(t, o, icbc::Decoder_AMD) +\n'
+                    '         icbc::evaluate_bc3_error(t, o, true) +\n'
+                    '         icbc::compress_bc3(icbc::Quality_Level4, c, w, cw, false, o);\n}\n')
         obj = os.path.join(tmp, "caller.o")
         subprocess.run([_cxx(), "-c", "-I", REF_HEADER_DIR, src, "-o", obj], check=True)
         need = subprocess.run(["nm", "-u", obj], capture_output=True, text=True, check=True).stdout.split()
@@ -78,6 +81,16 @@ def test_cpp_dropin_matches_oracle(gpu_lib):
         assert np.array_equal(blocks, ob), lv
         assert np.array_equal(errs.view(np.uint32), oe.view(np.uint32)), lv
     rec = data[pos:pos + 96 * 68].reshape(96, 68)
+    pos += 96 * 68
     assert np.array_equal(rec[:, :64], O.decode_bc1(blocks, decoder))
     ev = rec[:, 64:].copy().view(np.float32).reshape(96)
     assert np.array_equal(ev.view(np.uint32), O.evaluate_bc1_error(rgba.reshape(96, 64), blocks, decoder).view(np.uint32))
+    # BC3 as the reference has it: decode / evaluate, and compress_bc3 = 0 with the block untouched
+    i = np.arange(96, dtype=np.uint8)
+    bc3 = np.concatenate([i[:, None], (255 - i)[:, None], np.repeat(i[:, None], 6, 1), blocks], axis=1)
+    rec = data[pos:pos + 96 * 73].reshape(96, 73)
+    assert pos + 96 * 73 == data.size
+    assert np.array_equal(rec[:, :64], O.decode_bc3(bc3, decoder))
+    e3 = rec[:, 64:68].copy().view(np.float32).reshape(96)
+    assert np.array_equal(e3.view(np.uint32), O.evaluate_bc3_error(rgba.reshape(96, 64), bc3, True, decoder).view(np.uint32))
+    assert np.all(rec[:, 68:72].copy().view(np.float32) == 0.0) and np.all(rec[:, 72] == 1)

@@ -435,6 +435,19 @@ def test_decode_evaluate_golden(gpu_lib):
         assert same_bits(ig.evaluate_errors(rgba, blocks, d).cpu().numpy(), g["error_D%d" % d])
 
 
+def test_bc3_decode_evaluate_golden(gpu_lib):
+    import torch
+    ig = gpu_lib
+    g = np.load(os.path.join(GOLDEN, "bc3.npz"))
+    blocks = torch.from_numpy(g["blocks"]).cuda()
+    rgba = torch.from_numpy(g["rgba"]).cuda()
+    for d in range(4):
+        assert np.array_equal(ig.decode_bc3_blocks(blocks, d).cpu().numpy(), g["decoded_D%d" % d])
+        for ab in (0, 1):
+            e = ig.evaluate_bc3_errors(rgba, blocks, bool(ab), d).cpu().numpy()
+            assert same_bits(e, g["error_D%d_blend%d" % (d, ab)]), (d, ab)
+
+
 def test_host_buffer_path(gpu_lib):
     ig = gpu_lib
     img = synth.quality_sweep_image(200, 120, seed=2)

@@ -50,6 +50,17 @@ def test_oracle_decode_evaluate_golden():
         assert np.array_equal(e.view(np.uint32), g["error_D%d" % d].view(np.uint32))
 
 
+def test_oracle_bc3_golden():
+    """decode_bc3 / evaluate_bc3_error as the reference implements them
+    (4-colour palette, alpha0 everywhere), against its own outputs."""
+    g = np.load(os.path.join(GOLDEN, "bc3.npz"))
+    for d in range(4):
+        assert np.array_equal(O.decode_bc3(g["blocks"], d), g["decoded_D%d" % d])
+        for ab in (0, 1):
+            e = O.evaluate_bc3_error(g["rgba"], g["blocks"], ab, d)
+            assert np.array_equal(e.view(np.uint32), g["error_D%d_blend%d" % (d, ab)].view(np.uint32)), (d, ab)
+
+
 def test_image_path_equals_block_path():
     """Image encode (edge replication, u8/255, alpha weights) equals the block
     API on the gathered texels, for a size that is not a multiple of 4."""
