@@ -122,6 +122,8 @@ def load(build_if_missing: bool = True):
             "icbc_gpu_compress_bc1_images_each": (i32, [ctypes.POINTER(ImageDesc), i32, vp]),
             "icbc_gpu_decode_bc1": (i32, [vp, vp, i64, i32, vp]),
             "icbc_gpu_evaluate_bc1_error": (i32, [vp, vp, vp, i64, i32, vp]),
+            "icbc_gpu_decode_bc3": (i32, [vp, vp, i64, i32, vp]),
+            "icbc_gpu_evaluate_bc3_error": (i32, [vp, vp, vp, i64, i32, i32, vp]),
             "icbc_gpu_compress_bc1_image_host": (i32, [vp, i32, i32, i64, i32, vp, i32, i32, i32, i32, f32p, vp, vp]),
             "icbc_gpu_debug_tables": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
             "icbc_gpu_server_create": (i32, [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]),

@@ -15,6 +15,12 @@
 // every GPU that loads this library holds them (about 38 KB) until the process
 // exits.  The caller passes device inputs and outputs as for the other forms.
 //
+// A call plans its queue on the host in one static staging record (guarded by
+// a mutex, so no stack or heap is used for it) and hands it to the GPU as the
+// by-value parameter of a small staging kernel, which writes it into the
+// array and clears the counter; the encode kernel follows in stream order.
+// Nothing on the GPU refers to host memory of the call once it has returned.
+//
 // All calls share the one array and it keeps the last call's contents: each
 // call rewrites the descriptors and offsets it uses and clears the counter.
 // Calls whose GPU work overlaps (different streams without ordering, or two
@@ -43,6 +49,27 @@ struct NoAllocQueue {
 // cudaGetSymbolAddress at set-up.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocQueue)];
 static __device__ __align__(16) GlobalTables g_noalloc_tables;
+
+// One call's queue as planned on the host: passed by value as a kernel
+// parameter (within the 32,764-byte parameter limit), so the launch itself
+// carries it to the device.
+struct NoAllocPlan {
+    ImageDesc images[ICBC_GPU_NOALLOC_MAX_IMAGES];
+    uint32_t task_start[ICBC_GPU_NOALLOC_MAX_IMAGES + 1];
+    int n_images;
+};
+static_assert(sizeof(NoAllocPlan) <= 32000, "the plan must fit in a kernel parameter");
+
+// Writes the plan's first n_images descriptors and n_images + 1 offsets into
+// the scratch array and clears the queue counter (device code names the array
+// directly).
+__global__ void k_noalloc_stage(const __grid_constant__ NoAllocPlan plan) {
+    NoAllocQueue *q = reinterpret_cast<NoAllocQueue *>(g_noalloc_scratch);
+    const int n = plan.n_images;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) q->images[i] = plan.images[i];
+    for (int i = threadIdx.x; i <= n; i += blockDim.x) q->task_start[i] = plan.task_start[i];
+    if (threadIdx.x == 0) q->counter = 0;
+}
 
 // Same work loop as k_encode_batch, with tasks found from per-image offsets
 // instead of an allocated task list: task t belongs to the last image whose
@@ -151,16 +178,25 @@ int setup_current_device(DeviceState *out) {
 
 using namespace icbc_gpu;
 
+namespace {
+// The host staging record of every call (about 27 KB), outside any stack.
+std::mutex g_plan_mutex;
+icbc_gpu::NoAllocPlan g_plan;
+}  // namespace
+
 extern "C" int icbc_gpu_compress_bc1_images_noalloc(const icbc_gpu_image *images, int n_images, void *stream) {
     if (n_images < 0 || (n_images > 0 && !images)) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     if (n_images > ICBC_GPU_NOALLOC_MAX_IMAGES) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     if (n_images == 0) return ICBC_GPU_OK;
-    // Descriptors and offsets are built on the stack, most expensive level
-    // first (larger images first inside a level), as the allocated batch does.
-    ImageDesc descs[ICBC_GPU_NOALLOC_MAX_IMAGES];
-    uint32_t start[ICBC_GPU_NOALLOC_MAX_IMAGES + 1];
+    DeviceState S;
+    int st = setup_current_device(&S);
+    if (st) return st;
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    // Descriptors most expensive level first (larger images first inside a
+    // level), as the allocated batch orders them, then each image's first task.
+    ImageDesc *descs = g_plan.images;
     for (int i = 0; i < n_images; i++) {
-        const int st = resolve_image_desc(images[i], descs[i]);
+        st = resolve_image_desc(images[i], descs[i]);
         if (st) return st;
     }
     for (int i = 1; i < n_images; i++) {
@@ -175,22 +211,17 @@ extern "C" int icbc_gpu_compress_bc1_images_noalloc(const icbc_gpu_image *images
     }
     int64_t total = 0;
     for (int i = 0; i < n_images; i++) {
-        start[i] = (uint32_t)total;
+        g_plan.task_start[i] = (uint32_t)total;
         total += (descs[i].nblocks + 31) / 32;
         if (total > 0x7fffffff) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     }
-    start[n_images] = (uint32_t)total;
+    g_plan.task_start[n_images] = (uint32_t)total;
+    g_plan.n_images = n_images;
 
-    DeviceState S;
-    int st = setup_current_device(&S);
-    if (st) return st;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    // Host -> device copies of stack buffers: from pageable memory the call
-    // returns after the source has been staged, so the stack may be reused.
-    cudaError_t e = cudaMemcpyAsync(S.queue->images, descs, sizeof(ImageDesc) * n_images, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(S.queue->task_start, start, sizeof(uint32_t) * (n_images + 1), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(&S.queue->counter, 0, sizeof(int), s);
+    // The launch copies the plan; g_plan may be rewritten once it returns.
+    k_noalloc_stage<<<1, 256, 0, s>>>(g_plan);
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
     k_encode_batch_noalloc<<<S.grid, kWarpsPerCta * 32, smem_bytes(true), s>>>(S.queue, n_images, (int)total);
     e = cudaGetLastError();

@@ -186,6 +186,10 @@ int icbc_gpu_compress_bc1_images_each(const icbc_gpu_image *images, int n_images
  *     make that first call before any stream capture.  icbc_gpu_init is not
  *     needed unless an image uses ICBC_GPU_DECODER_DEFAULT.
  *   - Asynchronous on `stream`; `images` may be reused once the call returns.
+ *     The queue is planned in a static host record (about 27 KB, not on the
+ *     caller's stack) and reaches the device as a kernel parameter, so no
+ *     host memory of the call is read after it returns; host threads take
+ *     turns on that record.
  *   - Every call shares the one array and each call clears its queue counter.
  *     Calls whose GPU work overlaps (unordered streams, concurrent host
  *     threads) race on the array and corrupt each other: order them. */
