@@ -60,14 +60,13 @@ REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
 # DRAM bytes per level call (dram__bytes_read.sum + dram__bytes_write.sum of
 # its launches: the first pass, the listed pass and, at level 9, the
 # refinement pass) from one ncu capture of this workload without cache
-# flushes between kernels, as a timed call runs, summarised in
-# profiles/k_image_listed_L8_L9_k_refine_quality_sweep_4096.md.  Level 8's
+# flushes between kernels, as a timed call runs.  Level 8's
 # figure includes ~46 MB of write-backs of the buffer that flushes L2 before
 # the step; level 9's is its own traffic (the image is read once, through L2).
 NCU_TRAFFIC_BYTES = {8: (67.19e6 + 46.57e6) + (21.31e6 + 12.40e6),
                      9: (16.95e6 + 9.31e6) + (22.70e6 + 7.58e6) + (13.98e6 + 8.31e6)}
-TRAFFIC_SOURCE = "ncu --cache-control none, dram__bytes_read.sum + dram__bytes_write.sum per level call, " \
-                 "profiles/k_image_listed_L8_L9_k_refine_quality_sweep_4096.md"
+TRAFFIC_SOURCE = "one ncu capture of this workload with --cache-control none: dram__bytes_read.sum + " \
+                 "dram__bytes_write.sum summed over the level call's launches"
 
 
 def launches_per_level(level: int) -> int:
@@ -185,6 +184,45 @@ def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=None):
     return times, stats, outs
 
 
+def block_texels(img: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """RGBA8 texels (len(idx), 64) of blocks idx (row-major block order) with
+    edge replication, as the encoder reads them."""
+    h, w = img.shape[:2]
+    bw = (w + 3) // 4
+    by, bx = np.asarray(idx) // bw, np.asarray(idx) % bw
+    ys = np.minimum(by[:, None] * 4 + np.arange(4)[None, :], h - 1)
+    xs = np.minimum(bx[:, None] * 4 + np.arange(4)[None, :], w - 1)
+    return np.ascontiguousarray(img[ys[:, :, None], xs[:, None, :]].reshape(len(idx), 64))
+
+
+def parity(gpu: np.ndarray, ref: np.ndarray, img: np.ndarray, decoder: int) -> dict:
+    """Bit-exactness of every block against the oracle: the mismatch count and,
+    over mismatching blocks, the worst relative difference of their
+    evaluate_bc1_error (icbc.h:3030-3046) from the oracle block's."""
+    from oracle import oracle as O
+    bad = np.flatnonzero((gpu.reshape(-1, 8) != ref.reshape(-1, 8)).any(1))
+    worst = 0.0
+    if bad.size:
+        tex = block_texels(img, bad)
+        eg = O.evaluate_bc1_error(tex, gpu.reshape(-1, 8)[bad], decoder).astype(np.float64)
+        er = O.evaluate_bc1_error(tex, ref.reshape(-1, 8)[bad], decoder).astype(np.float64)
+        worst = float(np.max(np.abs(eg - er) / np.maximum(er, 1e-30)))
+    return {"blocks_checked": int(gpu.size // 8), "mismatches": int(bad.size), "worst_rel_error_delta": worst}
+
+
+def rmse_psnr(img: np.ndarray, blocks: np.ndarray, decoder: int):
+    """RMSE and PSNR of an encoded image from the oracle's FP64 decode and
+    compare over every block texel, as icbc_test.cpp:309-324 computes them:
+    mse = sum of evaluate_bc1_error / (16 * blocks), PSNR clamped to
+    [0, 300] dB (1e10 for an exact image)."""
+    from oracle import oracle as O
+    nb = blocks.size // 8
+    mse = O.image_sse(img, blocks, decoder) / (16.0 * nb)
+    rms = float(np.sqrt(mse))
+    psnr = float(min(max(20.0 * np.log10(255.0 / rms), 0.0), 300.0)) if rms > 0 else 1e10
+    return rms, psnr, mse
+
+
 def max_over_ranks(value: float, device) -> float:
     """The largest of every rank's value (the job's time is its slowest rank)."""
     import torch
@@ -205,6 +243,21 @@ def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def sample_text(stride: int, px: int) -> str:
+    if stride == 1:
+        return "the whole workload: all 10 levels of the image (%d px per level)" % px
+    return "every %dth block row of the workload (%d px per level), all 10 levels" % (stride, px)
+
+
+def sweep_config(size: int, ws: int) -> dict:
+    """The workload's config, the same in both arms' lines."""
+    return {"workload": "quality_sweep_%dx%d_L0-9" % (size, size), "levels": LEVELS, "color_weights": CW,
+            "input_weights": "alpha/255", "decoder": "D3D10", "three_color_mode": True, "three_color_black": True,
+            "form": "plain: one call per level (1 launch at levels 0-1, 2 at levels 2-8, 3 at level 9)",
+            "l2": "flushed between steps (256 MB write outside the timed events)",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
 
 
 def run_reference(args):
@@ -231,13 +284,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "quality_sweep_%dx%d_L0-9" % (args.size, args.size), "levels": LEVELS,
-                   "color_weights": CW, "input_weights": "alpha/255", "decoder": "D3D10",
-                   "three_color_mode": True, "three_color_black": True,
-                   "sample": "every %dth row of 4x4 blocks (%d px per level)" % (args.cpu_stride, px)},
+        "config": sweep_config(args.size, ws),
         "per_level": {str(lv): len(per_level[lv]) and px / statistics.mean(per_level[lv]) / 1e9 for lv in LEVELS},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": "every %dth block row of the workload, all 10 levels" % args.cpu_stride},
+                         "sample": sample_text(args.cpu_stride, px)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -314,9 +364,9 @@ def run_ours(args):
     value = whole_job_gpix(ws, len(LEVELS) * px, step_ms)
 
     # End to end through the host-buffer C-ABI call: pinned image in, blocks out.
-    e2e_value = h2d = d2h = None
+    e2e = None
     if not args.no_e2e:
-        e2e_value, h2d, d2h = e2e_leg(ig, torch, img, nb, px, ws, args)
+        e2e = e2e_leg(ig, torch, img, nb, px, ws, args)
     if rank != 0:
         return
     batch = None if (args.no_batch or args.no_cpu_baseline) else batch_leg(ig, torch, dev, args)
@@ -326,20 +376,27 @@ def run_ours(args):
     if args.no_cpu_baseline:
         print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                           "warmup": args.warmup, "ms_per_step": step_ms, "levels": LEVELS,
-                          "per_level_ms": lvl_ms, "e2e": e2e_value, "clocks": clk, "profiling_run": True}))
+                          "per_level_ms": lvl_ms, "e2e": e2e and e2e["value"], "clocks": clk,
+                          "profiling_run": True}))
         return
-    # CPU baseline + algorithmic op counts + sampled parity on every level.
-    sample = sample_rows(img, args.cpu_stride)
+    # CPU baseline, algorithmic op counts and complete parity: the oracle
+    # encodes the workload (every block of every level; stride 1 by default)
+    # on every host thread, timed as the CPU baseline, and every GPU block is
+    # compared with it, outside the timed region.
+    sample = img if args.cpu_stride == 1 else sample_rows(img, args.cpu_stride)
     sample_px = sample.shape[0] * sample.shape[1]
     nthreads = os.cpu_count() or 1
     ctimes, cstats, couts = cpu_sweep(sample, nthreads, levels=LEVELS)
     cpu_value = len(LEVELS) * sample_px / sum(ctimes.values()) / 1e9
     bw = w // 4
     rows = list(range(0, h // 4, args.cpu_stride))
-    mismatches = {}
+    checks, quality = {}, {}
     for lv in LEVELS:
-        gpu = outs[lv].cpu().numpy().reshape(h // 4, bw, 8)[rows].reshape(-1, 8)
-        mismatches[str(lv)] = int((gpu != couts[lv]).any(1).sum())
+        gpu = outs[lv].cpu().numpy()
+        gsample = gpu.reshape(h // 4, bw, 8)[rows].reshape(-1, 8)
+        checks[str(lv)] = parity(gsample, couts[lv], sample, 0)
+        rms, psnr, _ = rmse_psnr(img, gpu, 0)
+        quality[str(lv)] = {"rmse": rms, "psnr_db": psnr}
     scale = nb / cstats[LEVELS[0]]["blocks"]
     ops = {lv: algorithmic_ops(cstats[lv], lv) * scale for lv in LEVELS}
     peaks = load_peaks()
@@ -356,13 +413,14 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "quality_sweep_%dx%d_L0-9" % (w, h), "levels": LEVELS, "color_weights": CW,
-                   "input_weights": "alpha/255", "decoder": "D3D10", "three_color_mode": True,
-                   "three_color_black": True, "form": "plain (one launch per level)",
-                   "l2": "flushed between steps (256 MB write outside the timed events)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": sweep_config(w, ws),
         "per_level": per_level,
-        "mismatches_sampled": mismatches,
+        "parity": {"against": "oracle (C restatement of the reference's scalar encoder, pinned to the compiled "
+                              "reference)", "per_level": checks,
+                   "blocks_checked": sum(c["blocks_checked"] for c in checks.values()),
+                   "mismatches": sum(c["mismatches"] for c in checks.values())},
+        "quality": {"how": "FP64 decode-and-compare of the GPU blocks (oracle decode): RMSE and PSNR per level "
+                           "image, icbc_test.cpp:309-324", "per_level": quality},
         "roofline": {"bound": "fp32", "kernel": level_kernels(top), "achieved": achieved, "peak": peak,
                      "unit": "Tops/s", "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES.get(top),
                      "traffic_unit": "bytes per level call", "traffic_source": TRAFFIC_SOURCE,
@@ -372,9 +430,11 @@ def run_ours(args):
                                  "unit": "GB/s", "frac": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9 / hbm,
                                  "traffic": None} if 0 in lvl_ms else None),
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": "every %dth block row (%d px) at all 10 levels" % (args.cpu_stride, sample_px)},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step"},
+                         "sample": sample_text(args.cpu_stride, sample_px)},
+        "e2e": {"value": e2e["value"] if e2e else None, "unit": UNIT,
+                "h2d_bytes_per_step": e2e["h2d"] if e2e else None, "d2h_bytes_per_step": e2e["d2h"] if e2e else None,
+                "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step",
+                "steps": e2e["steps"] if e2e else None, "ms_per_step_min_max": e2e["min_max"] if e2e else None},
         "autotune": tuning,
         "batch": batch,
         "serving": serving,
@@ -388,23 +448,27 @@ def run_ours(args):
 
 def e2e_leg(ig, torch, img, nb, px, ws, args):
     """Same metric through the host-buffer C-ABI call: pinned image in, blocks
-    out, host<->device copies inside the timed region."""
+    out, host<->device copies inside the timed region; as many steps as the
+    device-timed leg, each step's wall time taken separately."""
     pin = torch.from_numpy(img).pin_memory()
     host_img = pin.numpy()
     host_out = {lv: torch.zeros((nb, 8), dtype=torch.uint8).pin_memory().numpy() for lv in LEVELS}
     for lv in LEVELS:
         ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
-    steps = max(2, min(args.steps, 5))
-    t0 = time.perf_counter()
+    steps = max(3, args.steps)
+    times = []
     for _ in range(steps):
+        t0 = time.perf_counter()
         for lv in LEVELS:
             ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
-    t = (time.perf_counter() - t0) / steps
+        times.append(time.perf_counter() - t0)
+    t = statistics.mean(times)
     if ws > 1:  # the job's time is its slowest rank's
         t = max_over_ranks(t * 1e3, torch.device("cuda", torch.cuda.current_device())) * 1e-3
     h2d = len(LEVELS) * img.nbytes + sum(nb * 8 for lv in LEVELS if lv >= 4)
     d2h = len(LEVELS) * nb * 8
-    return ws * len(LEVELS) * px / t / 1e9, h2d, d2h
+    return {"value": ws * len(LEVELS) * px / t / 1e9, "h2d": h2d, "d2h": d2h, "steps": steps,
+            "min_max": [min(times) * 1e3, max(times) * 1e3]}
 
 
 def batch_leg(ig, torch, dev, args):
@@ -415,14 +479,15 @@ def batch_leg(ig, torch, dev, args):
     (one persistent launch, replayed graph), checks both give the same bytes."""
     from icbc_gb300 import synth
     specs = synth.batch_specs(args.batch_images, seed=7)
-    bases = [torch.from_numpy(synth.gradient_noise_rects(2048, 2048, 100 + k)).to(dev) for k in range(4)]
-    imgs, outs_plain, outs_batch, descs = [], [], [], []
+    host_bases = [synth.gradient_noise_rects(2048, 2048, 100 + k) for k in range(4)]
+    bases = [torch.from_numpy(b).to(dev) for b in host_bases]
+    imgs, outs_plain, outs_batch, descs, crops = [], [], [], [], []
     px = 0
     for i, s in enumerate(specs):
-        base = bases[i % len(bases)]
         y0 = (s.seed * 131) % (2049 - s.height)
         x0 = (s.seed * 197) % (2049 - s.width)
-        img = base[y0:y0 + s.height, x0:x0 + s.width].contiguous()
+        img = bases[i % len(bases)][y0:y0 + s.height, x0:x0 + s.width].contiguous()
+        crops.append((i % len(bases), y0, x0))
         nb = ig.blocks_of(s.width, s.height)
         imgs.append(img)
         outs_plain.append(torch.zeros((nb, 8), dtype=torch.uint8, device=dev))
@@ -456,18 +521,51 @@ def batch_leg(ig, torch, dev, args):
         ms = e0.elapsed_time(e1) / args.batch_steps
         res[name] = {"ms": ms, "gpix_s": px / (ms * 1e-3) / 1e9}
     batch.close()
-    # spot-check a few images against the oracle
+    # Every image against the oracle (all blocks), and its RMSE / PSNR from
+    # the FP64 decode-and-compare; one image per host thread at a time.
     from oracle import oracle as O
-    bad = 0
-    for i in range(0, len(specs), max(1, len(specs) // 6)):
+    O.lib()
+    host_out = [o.cpu().numpy() for o in outs_batch]
+
+    def check(i):
         s = specs[i]
-        ob, _ = O.encode_image(imgs[i].cpu().numpy(), s.level, s.decoder, (1, 1, 1), 0, None, True, True,
-                               nthreads=os.cpu_count() or 1)
-        bad += int((outs_batch[i].cpu().numpy() != ob).any(1).sum())
+        k, y0, x0 = crops[i]
+        img = np.ascontiguousarray(host_bases[k][y0:y0 + s.height, x0:x0 + s.width])
+        ob, _ = O.encode_image(img, s.level, s.decoder, (1, 1, 1), 0, None, True, True, nthreads=1)
+        pr = parity(host_out[i], ob, img, s.decoder)
+        rms, psnr, mse = rmse_psnr(img, host_out[i], s.decoder)
+        return pr, rms, psnr, mse
+
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        results = list(ex.map(check, range(len(specs))))
+    mism = sum(r[0]["mismatches"] for r in results)
+    worst = max(r[0]["worst_rel_error_delta"] for r in results)
+    psnrs = np.array([r[2] for r in results])
+    rmses = np.array([r[1] for r in results])
+    nbs = np.array([ig.blocks_of(s.width, s.height) for s in specs], np.float64)
+    agg_mse = float(np.sum([r[3] for r in results] * nbs) / nbs.sum())
+    by_level = {}
+    for lv in range(10):
+        sel = [i for i, s in enumerate(specs) if s.level == lv]
+        if sel:
+            m = float(np.sum([results[i][3] * nbs[i] for i in sel]) / nbs[sel].sum())
+            by_level[str(lv)] = {"images": len(sel), "rmse": float(np.sqrt(m)),
+                                 "psnr_db": float(20 * np.log10(255.0 / np.sqrt(m))) if m > 0 else 1e10}
+    q = lambda a, p: float(np.percentile(a, p))  # noqa: E731
     return {"workload": "mixed_batch_%d_images" % len(specs), "pixels": px,
             "plain": res["plain"], "batched": res["batched"],
             "speedup_batched_over_plain": res["plain"]["ms"] / res["batched"]["ms"],
-            "batched_equals_plain": bool(same), "oracle_mismatches_sampled": bad,
+            "batched_equals_plain": bool(same),
+            "parity": {"images_checked": len(specs), "blocks_checked": int(nbs.sum()), "mismatches": mism,
+                       "worst_rel_error_delta": worst},
+            "quality": {"how": "FP64 decode-and-compare per image (icbc_test.cpp:309-324), aggregate weighted by "
+                               "blocks as the reference driver sums it",
+                        "rmse": float(np.sqrt(agg_mse)), "psnr_db": float(20 * np.log10(255.0 / np.sqrt(agg_mse))),
+                        "per_image_rmse_min_p50_max": [float(rmses.min()), q(rmses, 50), float(rmses.max())],
+                        "per_image_psnr_min_p1_p50_p99_max": [float(psnrs.min()), q(psnrs, 1), q(psnrs, 50),
+                                                              q(psnrs, 99), float(psnrs.max())],
+                        "per_level": by_level},
             "launches_plain": len(specs), "launches_batched": 1}
 
 
@@ -562,17 +660,23 @@ def hard_leg(ig, torch, dev, args, peak_tops):
         res[name] = {"ms": ms, "gpix_s": n * side * side / (ms * 1e-3) / 1e9}
     batch.close()
     same = all(torch.equal(a, b) for a, b in zip(outs_b, outs_p))
-    # sampled oracle parity + op counts: every 97th block row of every 8th image
-    mism, sampled, stats = 0, 0, None
-    for i in range(0, n, 8):
+    # Oracle parity + op counts: every block of image 0, and every 97th block
+    # row of every 8th image after it.
+    nthreads = os.cpu_count() or 1
+    host0 = imgs[0].cpu().numpy()
+    ob, _, stats = O.encode_image(host0, 9, 0, cw, 1, None, True, True, nthreads=nthreads, with_stats=True)
+    full = parity(outs_b[0].cpu().numpy(), ob, host0, 0)
+    mism, sampled, worst = full["mismatches"], full["blocks_checked"], full["worst_rel_error_delta"]
+    for i in range(8, n, 8):
         host = imgs[i].cpu().numpy()
         rows = sample_rows(host, 97)
-        ob, _, st = O.encode_image(rows, 9, 0, cw, 1, None, True, True, nthreads=os.cpu_count() or 1,
-                                   with_stats=True)
+        ob, _, st = O.encode_image(rows, 9, 0, cw, 1, None, True, True, nthreads=nthreads, with_stats=True)
         gpu = outs_b[i].cpu().numpy().reshape(side // 4, side // 4, 8)[::97].reshape(-1, 8)
-        mism += int((gpu != ob).any(1).sum())
-        sampled += ob.shape[0]
-        stats = st if stats is None else {k: stats[k] + st[k] for k in st}
+        pr = parity(gpu, ob, rows, 0)
+        mism += pr["mismatches"]
+        sampled += pr["blocks_checked"]
+        worst = max(worst, pr["worst_rel_error_delta"])
+        stats = {k: stats[k] + st[k] for k in st}
     ops = algorithmic_ops(stats, 9) * (n * nb) / stats["blocks"]
     # FP64 decode-and-compare on the GPU: exact per-block integer SSE, FP64 sums
     psnr = []
@@ -594,7 +698,10 @@ def hard_leg(ig, torch, dev, args, peak_tops):
     return {"workload": "hard_mixture_%dx%d^2_L9" % (n, side), "blocks": n * nb,
             "batched": res["batched"], "plain": res["plain"],
             "speedup_batched_over_plain": res["plain"]["ms"] / res["batched"]["ms"],
-            "batched_equals_plain": bool(same), "oracle_sampled_blocks": sampled, "oracle_mismatches": mism,
+            "batched_equals_plain": bool(same),
+            "parity": {"blocks_checked": sampled, "mismatches": mism, "worst_rel_error_delta": worst,
+                       "images_checked_whole": 1, "full_image_0": full,
+                       "also": "every 97th block row of images 8, 16, ..., %d" % (8 * ((n - 1) // 8))},
             "rmse": float(np.sqrt(mse)), "psnr_db": float(20 * np.log10(255.0 / np.sqrt(mse))),
             "psnr_db_per_image_min_max": [float(min(psnr)), float(max(psnr))],
             "fp64_sse_image0_gpu_vs_oracle": [ev0, sse0],
@@ -608,7 +715,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=4096)
-    ap.add_argument("--cpu-stride", type=int, default=8)
+    ap.add_argument("--cpu-stride", type=int, default=1,
+                    help="the CPU legs encode every n-th block row (1: the whole workload)")
     ap.add_argument("--levels", type=int, nargs="+", default=None,
                     help="encode only these levels (profiling); the headline uses all ten")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")

@@ -458,27 +458,33 @@ def test_host_buffer_path(gpu_lib):
         assert np.array_equal(out, ob) and same_bits(errs, oe)
 
 
-@pytest.mark.parametrize("level", [0, 8, 9])
-def test_full_size_sampled_parity(gpu_lib, level):
-    """4096x4096 quality-sweep image: every 61st block checked against the
-    oracle, plus decode->evaluate consistency over the whole image."""
+@pytest.fixture(scope="module")
+def sweep_image():
+    return synth.quality_sweep_image(4096, 4096, seed=1)
+
+
+@pytest.mark.parametrize("level", range(10))
+def test_full_size_parity(gpu_lib, sweep_image, level):
+    """The 4096x4096 quality-sweep workload (alpha weights, luma colour
+    weights, D3D10): every block and every returned error equals the
+    oracle's, at every level; the GPU's decode + evaluate over the whole image
+    equals the oracle's FP64 decode-and-compare."""
     import torch
     ig = gpu_lib
-    img = synth.quality_sweep_image(4096, 4096, seed=1)
+    img = sweep_image
     cw = (0.299, 0.587, 0.114)
-    out = ig.compress_image(_to_dev(img), level, 0, cw, weight_mode=ig.WEIGHTS_ALPHA)
+    out, err = ig.compress_image(_to_dev(img), level, 0, cw, weight_mode=ig.WEIGHTS_ALPHA, with_errors=True)
     blocks = out.cpu().numpy()
-    cols, w, tex = O.image_blocks(img, weight_mode=1)
-    idx = np.arange(0, blocks.shape[0], 61)
-    ob, _ = O.compress_blocks(cols[idx], w[idx], level, 0, cw, True, True, nthreads=8)
-    assert np.array_equal(blocks[idx], ob)
-    # whole image: GPU decode + evaluate equals the oracle's on a sample, and PSNR is sane
+    ob, oe = O.encode_image(img, level, 0, cw, 1, None, True, True, nthreads=os.cpu_count() or 1)
+    bad = np.flatnonzero((blocks != ob).any(1))
+    assert bad.size == 0, (level, bad[:10])
+    assert same_bits(err.cpu().numpy(), oe)
+    _, _, tex = O.image_blocks(img, weight_mode=1)
     rgba = torch.from_numpy(np.ascontiguousarray(tex.reshape(-1, 64))).cuda()
     e = ig.evaluate_errors(rgba, out, 0).cpu().numpy()
-    oe = O.evaluate_bc1_error(tex[idx].reshape(-1, 64), blocks[idx], 0)
-    assert same_bits(e[idx], oe)
-    mse = e.astype(np.float64).sum() / (16 * blocks.shape[0])
-    assert 20 * np.log10(255 / np.sqrt(mse)) > 30
+    sse = e.astype(np.float64).sum()
+    assert sse == O.image_sse(img, blocks, 0)
+    assert 20 * np.log10(255 / np.sqrt(sse / (16 * blocks.shape[0]))) > 30
 
 
 def test_launch_shapes_do_not_change_results(gpu_lib):
