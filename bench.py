@@ -308,6 +308,10 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     ig.init(ig.Decoder_D3D10)
     sms = ig.load().icbc_gpu_sm_count()
+    if args.only_hard:  # profiling runs of the hard-mixture leg alone
+        peak = fp32_peak_tops(load_peaks(), sms)
+        print(json.dumps({"hard": hard_leg(ig, torch, dev, args, peak), "profiling_run": True}))
+        return
 
     img = synth.quality_sweep_image(args.size, args.size, seed=1)
     h, w = img.shape[:2]
@@ -660,6 +664,11 @@ def hard_leg(ig, torch, dev, args, peak_tops):
         res[name] = {"ms": ms, "gpix_s": n * side * side / (ms * 1e-3) / 1e9}
     batch.close()
     same = all(torch.equal(a, b) for a, b in zip(outs_b, outs_p))
+    if args.no_parity:
+        del imgs, outs_b, outs_p
+        torch.cuda.empty_cache()
+        return {"workload": "hard_mixture_%dx%d^2_L9" % (n, side), "blocks": n * nb, "batched": res["batched"],
+                "plain": res["plain"], "batched_equals_plain": bool(same)}
     # Oracle parity + op counts: every block of image 0, and every 97th block
     # row of every 8th image after it.
     nthreads = os.cpu_count() or 1
@@ -730,6 +739,9 @@ def main():
     ap.add_argument("--hard-images", type=int, default=64)
     ap.add_argument("--hard-side", type=int, default=8192)
     ap.add_argument("--hard-steps", type=int, default=2)
+    ap.add_argument("--only-hard", action="store_true", help="run the hard-mixture leg alone (profiling)")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="with --only-hard: skip the oracle checks and op counts (profiling)")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 5000, 20000])
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-max-requests", type=int, default=4000)

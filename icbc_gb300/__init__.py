@@ -32,6 +32,7 @@ WEIGHTS_UNIFORM, WEIGHTS_ALPHA, WEIGHTS_PLANE = 0, 1, 2
 NOALLOC_MAX_IMAGES = 256
 # SIMD builds of the reference whose output the *_simd entry points reproduce.
 SIMD_SCALAR, SIMD_SSE2, SIMD_SSE41, SIMD_AVX, SIMD_AVX2, SIMD_AVX512 = 0, 1, 2, 3, 4, 5
+SIMD_NEON = -1  # ICBC_SIMD's value for NEON (icbc.h:65)
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "not initialized", 3: "CUDA error", 4: "out of memory",
           5: "misaligned", 6: "over budget", 7: "not ready", 8: "cancelled", 9: "not found"}

@@ -74,8 +74,9 @@ struct EncodeParams {
     V3 cw;
     // SIMD profile of the reference build reproduced by the profile kernels
     // (bc1_simd.cu): vector width of the cluster loops, fused vmadd/vmsub,
-    // vround01 half to even.  The plain kernels ignore these.
-    int simd_vec, simd_fma, simd_rne;
+    // vround01 half to even, vsaturate keeping a NaN (NEON).  The plain
+    // kernels ignore these.
+    int simd_vec, simd_fma, simd_rne, simd_nan;
 };
 
 // Everything one warp needs for a group of 32 blocks.
@@ -571,10 +572,13 @@ __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, cons
 
 // ----------------------------------------------- SIMD-profile cluster fit --
 //
-// The reference's SIMD builds (ICBC_SIMD 1..5, icbc.h:427-1369) run the same
-// cluster loops with vmadd / vmsub fused on AVX2 and AVX-512 (icbc.h:734-752,
-// :970-976) and vround01 rounding half to even from SSE4.1 on (icbc.h:518-524,
-// :764-766, :988-990).  These are cf4_combo / cf3_combo with those two choices.
+// The reference's SIMD builds (ICBC_SIMD 1..5 and -1, icbc.h:427-1235) run the
+// same cluster loops with vmadd / vmsub fused on AVX2 and AVX-512
+// (icbc.h:734-752, :970-976), vround01 rounding half to even from SSE4.1 on
+// and on NEON (icbc.h:518-524, :764-766, :988-990, :1159-1162), and, on NEON
+// only, a vsaturate that keeps a NaN (vmaxq_f32 / vminq_f32 return NaN for a
+// NaN operand, icbc.h:1155-1157; the x86 max / min return the other operand).
+// These are cf4_combo / cf3_combo with those three choices.
 __device__ __forceinline__ float pm_madd(bool f, float a, float b, float c) {
     return f ? __fmaf_rn(a, b, c) : a * b + c;
 }
@@ -584,20 +588,21 @@ __device__ __forceinline__ float pm_msub(bool f, float a, float b, float c) {
 // vm2sub(a, b, c, d) = vmsub(a, b, c * d) (icbc.h:415, :754-756, :978-980).
 __device__ __forceinline__ float pm_m2sub(bool f, float a, float b, float c, float d) { return pm_msub(f, a, b, c * d); }
 // vround5 / vround6 of a saturated value: int(t + 0.5f) or round-half-even
-// of t = x * n, both exact for 0 <= t < 2^23 through the 2^23 addition.
-__device__ __forceinline__ float pm_round(float x, float n, float inv_n, bool rne) {
-    const float t = __saturatef(x) * n;
+// of t = x * n, both exact for 0 <= t < 2^23 through the 2^23 addition (a
+// NaN, kept by NEON's vsaturate, stays NaN through both).
+__device__ __forceinline__ float pm_round(float x, float n, float inv_n, bool rne, bool nan) {
+    const float t = ((nan && x != x) ? x : __saturatef(x)) * n;
     const float r = rne ? __fsub_rn(__fadd_rn(t, 8388608.0f), 8388608.0f) : snap_floor(t + 0.5f);
     return r * inv_n;
 }
-__device__ __forceinline__ V3 pm_round_ept(V3 v, bool rne) {
-    return v3(pm_round(v.x, 31.0f, 1.0f / 31.0f, rne), pm_round(v.y, 63.0f, 1.0f / 63.0f, rne),
-              pm_round(v.z, 31.0f, 1.0f / 31.0f, rne));
+__device__ __forceinline__ V3 pm_round_ept(V3 v, bool rne, bool nan) {
+    return v3(pm_round(v.x, 31.0f, 1.0f / 31.0f, rne, nan), pm_round(v.y, 63.0f, 1.0f / 63.0f, rne, nan),
+              pm_round(v.z, 31.0f, 1.0f / 31.0f, rne, nan));
 }
 
 // cluster_fit_four's iteration (icbc.h:2685-2733) under a SIMD profile.
 __device__ __forceinline__ float cf4_combo_simd(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
-                                               bool f, bool rne, V3 &a, V3 &b) {
+                                               bool f, bool rne, bool nan, V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
     const float4 s0 = ld4(S + 4 * i0), s1 = ld4(S + 4 * i1), s2 = ld4(S + 4 * i2);
     V3 x0 = xyz(s0), x1 = xyz(s1), x2 = xyz(s2);
@@ -617,9 +622,9 @@ __device__ __forceinline__ float cf4_combo_simd(const float *S, uint32_t packed,
                      pm_madd(f, x2.z, q.w1_3, pm_madd(f, x1.z, q.w2_3, x0.z)));
     const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
     a = pm_round_ept(v3(pm_m2sub(f, ax.x, beta2, bx.x, ab) * factor, pm_m2sub(f, ax.y, beta2, bx.y, ab) * factor,
-                        pm_m2sub(f, ax.z, beta2, bx.z, ab) * factor), rne);
+                        pm_m2sub(f, ax.z, beta2, bx.z, ab) * factor), rne, nan);
     b = pm_round_ept(v3(pm_m2sub(f, bx.x, alpha2, ax.x, ab) * factor, pm_m2sub(f, bx.y, alpha2, ax.y, ab) * factor,
-                        pm_m2sub(f, bx.z, alpha2, ax.z, ab) * factor), rne);
+                        pm_m2sub(f, bx.z, alpha2, ax.z, ab) * factor), rne, nan);
     const V3 e2 = v3(pm_m2sub(f, a.x, pm_msub(f, b.x, ab, ax.x), b.x, bx.x) * 2.0f,
                      pm_m2sub(f, a.y, pm_msub(f, b.y, ab, ax.y), b.y, bx.y) * 2.0f,
                      pm_m2sub(f, a.z, pm_msub(f, b.z, ab, ax.z), b.z, bx.z) * 2.0f);
@@ -631,7 +636,7 @@ __device__ __forceinline__ float cf4_combo_simd(const float *S, uint32_t packed,
 
 // cluster_fit_three's iteration (icbc.h:2299-2323) under a SIMD profile.
 __device__ __forceinline__ float cf3_combo_simd(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
-                                               bool f, bool rne, V3 &a, V3 &b) {
+                                               bool f, bool rne, bool nan, V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
     const float4 s0 = ld4(S + 4 * i0), s1 = ld4(S + 4 * i1);
     const V3 x0 = xyz(s0);
@@ -648,9 +653,9 @@ __device__ __forceinline__ float cf3_combo_simd(const float *S, uint32_t packed,
     const V3 ax = x0 + x1 * 0.5f;
     const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
     a = pm_round_ept(v3(pm_m2sub(f, ax.x, beta2, bx.x, ab) * factor, pm_m2sub(f, ax.y, beta2, bx.y, ab) * factor,
-                        pm_m2sub(f, ax.z, beta2, bx.z, ab) * factor), rne);
+                        pm_m2sub(f, ax.z, beta2, bx.z, ab) * factor), rne, nan);
     b = pm_round_ept(v3(pm_m2sub(f, bx.x, alpha2, ax.x, ab) * factor, pm_m2sub(f, bx.y, alpha2, ax.y, ab) * factor,
-                        pm_m2sub(f, bx.z, alpha2, ax.z, ab) * factor), rne);
+                        pm_m2sub(f, bx.z, alpha2, ax.z, ab) * factor), rne, nan);
     const V3 e2 = v3(pm_m2sub(f, a.x, pm_msub(f, b.x, ab, ax.x), b.x, bx.x) * 2.0f,
                      pm_m2sub(f, a.y, pm_msub(f, b.y, ab, ax.y), b.y, bx.y) * 2.0f,
                      pm_m2sub(f, a.z, pm_msub(f, b.z, ab, ax.z), b.z, bx.z) * 2.0f);
@@ -824,9 +829,11 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
         V3 a, b;
         float ea, eb;
         if (SIMD) {
-            const bool f = p->simd_fma != 0, rne = p->simd_rne != 0;
-            ea = FOUR ? cf4_combo_simd(A.S, pa, A.sums, q, f, rne, a, b) : cf3_combo_simd(A.S, pa, A.sums, q, f, rne, a, b);
-            eb = FOUR ? cf4_combo_simd(B.S, pb, B.sums, q, f, rne, a, b) : cf3_combo_simd(B.S, pb, B.sums, q, f, rne, a, b);
+            const bool f = p->simd_fma != 0, rne = p->simd_rne != 0, nan = p->simd_nan != 0;
+            ea = FOUR ? cf4_combo_simd(A.S, pa, A.sums, q, f, rne, nan, a, b)
+                      : cf3_combo_simd(A.S, pa, A.sums, q, f, rne, nan, a, b);
+            eb = FOUR ? cf4_combo_simd(B.S, pb, B.sums, q, f, rne, nan, a, b)
+                      : cf3_combo_simd(B.S, pb, B.sums, q, f, rne, nan, a, b);
         } else {
             ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
             eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
@@ -971,7 +978,9 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         if (need4) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
             if (my4 >= 0) {
-                if (SIMD) cf4_combo_simd(srow, w.T->four[my4], fit_sums(srow, count), q, p.simd_fma, p.simd_rne, a, b);
+                if (SIMD)
+                    cf4_combo_simd(srow, w.T->four[my4], fit_sums(srow, count), q, p.simd_fma, p.simd_rne, p.simd_nan,
+                                   a, b);
                 else cf4_combo(srow, w.T->four[my4], fit_sums(srow, count), q, a, b);
             }
             ferr = output_block4(w, row, p, a, b, f0, f1, fi);
@@ -997,7 +1006,9 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         if (need3) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
             if (my3 >= 0) {
-                if (SIMD) cf3_combo_simd(srow, w.T->three[my3], fit_sums(srow, count3), q, p.simd_fma, p.simd_rne, a, b);
+                if (SIMD)
+                    cf3_combo_simd(srow, w.T->three[my3], fit_sums(srow, count3), q, p.simd_fma, p.simd_rne,
+                                   p.simd_nan, a, b);
                 else cf3_combo(srow, w.T->three[my3], fit_sums(srow, count3), q, a, b);
             }
             uint32_t t0, t1, ti;

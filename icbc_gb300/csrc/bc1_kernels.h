@@ -137,6 +137,7 @@ cudaError_t launch_evaluate_bc3(const void *rgba, const void *blocks, float *err
 
 // Level-9 refinement pass (bc1_refine.cu) and its stream-ordered scratch.
 cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream);
+cudaError_t scratch_prepare();
 cudaError_t scratch_free(void *ptr, cudaStream_t stream);
 cudaError_t launch_refine(const GlobalTables *G, const ImageDesc *image, const BlocksSrc *blocks,
                           const EncodeParams &p, uint2 *out, float *errors, const RefineSlot *st, int64_t n,

@@ -185,28 +185,41 @@ cudaMemPool_t g_pool[64] = {};
 
 }  // namespace
 
-// Stream-ordered scratch from a library-owned pool of the current device
-// (freed memory stays cached in the pool for the next call).
-cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream) {
+// The library-owned pool of the current device, created on first use.
+static cudaError_t device_pool(cudaMemPool_t *out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    cudaMemPool_t pool;
-    {
-        std::lock_guard<std::mutex> lock(g_pool_mutex);
-        if (!g_pool[dev]) {
-            cudaMemPoolProps props = {};
-            props.allocType = cudaMemAllocationTypePinned;
-            props.location.type = cudaMemLocationTypeDevice;
-            props.location.id = dev;
-            e = cudaMemPoolCreate(&g_pool[dev], &props);
-            if (e != cudaSuccess) return e;
-            uint64_t keep = 1ull << 30;
-            cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
-        }
-        pool = g_pool[dev];
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        e = cudaMemPoolCreate(&g_pool[dev], &props);
+        if (e != cudaSuccess) return e;
+        uint64_t keep = 1ull << 30;
+        cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
     }
+    *out = g_pool[dev];
+    return cudaSuccess;
+}
+
+// Creates the pool of the current device if it does not exist yet.  Pool
+// creation is not allowed while a stream captures, so code that captures
+// launches which take scratch calls this first.
+cudaError_t scratch_prepare() {
+    cudaMemPool_t pool;
+    return device_pool(&pool);
+}
+
+// Stream-ordered scratch from a library-owned pool of the current device
+// (freed memory stays cached in the pool for the next call).
+cudaError_t scratch_alloc(void **ptr, size_t bytes, cudaStream_t stream) {
+    cudaMemPool_t pool;
+    const cudaError_t e = device_pool(&pool);
+    if (e != cudaSuccess) return e;
     return cudaMallocFromPoolAsync(ptr, bytes, pool, stream);
 }
 

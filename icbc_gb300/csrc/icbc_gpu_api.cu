@@ -203,15 +203,32 @@ EncodeParams make_params(int decoder, int tc, int tcb, const float cw[3]) {
     p.simd_vec = 1;
     p.simd_fma = 0;
     p.simd_rne = 0;
+    p.simd_nan = 0;
     return p;
 }
 
-// Cluster-loop parameters of the reference's SIMD builds (ICBC_SIMD 0..5,
-// icbc.h:59-64): vector width, fused vmadd/vmsub, vround01 half to even.
+// Cluster-loop parameters of the reference's SIMD builds (ICBC_SIMD 0..5 and
+// -1 = NEON, icbc.h:59-66): vector width, fused vmadd/vmsub, vround01 half to
+// even, vsaturate keeping a NaN.  Index = ICBC_SIMD, NEON last.
 struct SimdProfile {
-    int vec, fma, rne;
+    int vec, fma, rne, nan;
 };
-constexpr SimdProfile kSimdProfiles[6] = {{1, 0, 0}, {4, 0, 0}, {4, 0, 1}, {8, 0, 1}, {8, 1, 1}, {16, 1, 1}};
+constexpr SimdProfile kSimdProfiles[7] = {{1, 0, 0, 0}, {4, 0, 0, 0}, {4, 0, 1, 0}, {8, 0, 1, 0},
+                                          {8, 1, 1, 0}, {16, 1, 1, 0}, {4, 0, 1, 1}};
+constexpr int kSimdNeonIndex = 6;
+
+// Table index of an ICBC_GPU_SIMD_* value, or -1 when it is not one.
+static int simd_index(int profile) {
+    if (profile == ICBC_GPU_SIMD_NEON) return kSimdNeonIndex;
+    return profile >= 0 && profile <= 5 ? profile : -1;
+}
+
+static void set_simd(EncodeParams &p, int index) {
+    p.simd_vec = kSimdProfiles[index].vec;
+    p.simd_fma = kSimdProfiles[index].fma;
+    p.simd_rne = kSimdProfiles[index].rne;
+    p.simd_nan = kSimdProfiles[index].nan;
+}
 
 // Validates an image descriptor and resolves it for the kernels.
 int resolve_image(const icbc_gpu_image &im, ImageDesc &d) {
@@ -417,7 +434,8 @@ int icbc_gpu_compress_bc1_blocks(int level, const float *d_colors, const float *
 int icbc_gpu_compress_bc1_blocks_simd(int simd_profile, int level, const float *d_colors, const float *d_weights,
                                       const float color_weights[3], int three_color_mode, int three_color_black,
                                       int decoder, void *d_out, float *d_errors, int64_t n_blocks, void *stream) {
-    if (simd_profile < 0 || simd_profile > 5) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    const int si = simd_index(simd_profile);
+    if (si < 0) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     // The scalar profile, and levels without a cluster fit, are the plain path.
     if (simd_profile == 0 || level == 0 || level == 1)
         return icbc_gpu_compress_bc1_blocks(level, d_colors, d_weights, color_weights, three_color_mode,
@@ -435,9 +453,7 @@ int icbc_gpu_compress_bc1_blocks_simd(int simd_profile, int level, const float *
     st = ensure_device_tables(&G);
     if (st) return st;
     EncodeParams p = make_params(dec, three_color_mode, three_color_black, color_weights);
-    p.simd_vec = kSimdProfiles[simd_profile].vec;
-    p.simd_fma = kSimdProfiles[simd_profile].fma;
-    p.simd_rne = kSimdProfiles[simd_profile].rne;
+    set_simd(p, si);
     BlocksSrc src{d_colors, d_weights};
     cudaError_t e = launch_simd(G, nullptr, &src, p, reinterpret_cast<uint2 *>(d_out), d_errors, n_blocks, level,
                                 reinterpret_cast<cudaStream_t>(stream));
@@ -445,7 +461,8 @@ int icbc_gpu_compress_bc1_blocks_simd(int simd_profile, int level, const float *
 }
 
 int icbc_gpu_compress_bc1_image_simd(int simd_profile, const icbc_gpu_image *image, void *stream) {
-    if (simd_profile < 0 || simd_profile > 5 || !image) return ICBC_GPU_ERR_INVALID_ARGUMENT;
+    const int si = simd_index(simd_profile);
+    if (si < 0 || !image) return ICBC_GPU_ERR_INVALID_ARGUMENT;
     if (simd_profile == 0 || image->level == 0 || image->level == 1) return icbc_gpu_compress_bc1_image(image, stream);
     ImageDesc d;
     int st = resolve_image(*image, d);
@@ -455,9 +472,7 @@ int icbc_gpu_compress_bc1_image_simd(int simd_profile, const icbc_gpu_image *ima
     if (st) return st;
     if (d.nblocks == 0) return ICBC_GPU_OK;
     EncodeParams p = make_params(d.decoder, d.three_color_mode, d.three_color_black, d.cw);
-    p.simd_vec = kSimdProfiles[simd_profile].vec;
-    p.simd_fma = kSimdProfiles[simd_profile].fma;
-    p.simd_rne = kSimdProfiles[simd_profile].rne;
+    set_simd(p, si);
     cudaError_t e = launch_simd(G, &d, nullptr, p, d.out, d.errors, d.nblocks, d.level,
                                 reinterpret_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? ICBC_GPU_OK : set_cuda_error(e);
@@ -611,6 +626,9 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     // the first pass, when there is one; the level-9 refinement pass after
     // it) once.
     cudaStream_t cs = nullptr;
+    // The launches of images with their own kernels take stream-ordered
+    // scratch (captured as allocation nodes); its pool must exist first.
+    if (e == cudaSuccess && !own.empty()) e = scratch_prepare();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {

@@ -170,6 +170,20 @@ class ImageSpec:
     seed: int
 
 
+def extreme_weight_blocks(n: int, seed: int, levels: int = 8) -> tuple[np.ndarray, np.ndarray]:
+    """Blocks of dark colours (channels 0..levels-1) with per-texel weights
+    spread log-uniformly over 1e-30 .. 1e30: the weighted sums overflow and
+    degenerate cluster splits divide zero by zero, the inputs where the
+    reference's NEON build (whose vsaturate keeps a NaN) and its x86 builds
+    part ways.  Returns compress_bc1 inputs (n,16,4) and (n,16)."""
+    tex = randint(seed, 90, (n, 16, 3), 0, levels)
+    lut = (np.arange(256, dtype=np.float32) / np.float32(255.0)).astype(np.float32)
+    cols = np.ones((n, 16, 4), np.float32)
+    cols[:, :, :3] = lut[tex]
+    w = (10.0 ** (uniform(seed, 91, (n, 16)) * 60.0 - 30.0)).astype(np.float32)
+    return cols, w
+
+
 def batch_specs(n: int = 2000, seed: int = 7, lo: int = 64, hi: int = 2048) -> list[ImageSpec]:
     """Sizes log-uniform in [lo, hi] per side, rounded to multiples of 4 except
     10% left as is; level uniform 0..9; decoder uniform over D3D10/NVIDIA/AMD."""

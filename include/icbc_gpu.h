@@ -119,18 +119,20 @@ int icbc_gpu_compress_bc1_image(const icbc_gpu_image *image, void *stream);
  * the SIMD backend it was compiled with (ICBC_SIMD, icbc.h:59-117): the
  * cluster-fit loops (icbc.h:2089-2344, :2362-2742) run over vectors of 4, 8
  * or 16 combinations whose lanes keep their own minimum, fuse vmadd/vmsub on
- * AVX2 and AVX-512 (icbc.h:734-752, :970-976) and round vround01 half to
- * even from SSE4.1 on (icbc.h:518-524, :764-766, :988-990).  These entry
- * points reproduce the output of such a build compiled without FP
- * contraction (-ffp-contract=off), for callers whose stored assets came from
- * one.  Profile ICBC_GPU_SIMD_SCALAR (and levels 0-1, which have no cluster
- * fit) is the plain path.  Same arguments and results otherwise as
+ * AVX2 and AVX-512 (icbc.h:734-752, :970-976), round vround01 half to even
+ * from SSE4.1 on and on NEON (icbc.h:518-524, :764-766, :988-990,
+ * :1159-1162), and on NEON keep a NaN through vsaturate (vmaxq_f32 /
+ * vminq_f32, icbc.h:1155-1157).  These entry points reproduce the output of
+ * such a build compiled without FP contraction (-ffp-contract=off; for NEON
+ * that makes vmlaq_f32 / vmlsq_f32 a multiply then an add, icbc.h:1142-1153),
+ * for callers whose stored assets came from one.  Profile
+ * ICBC_GPU_SIMD_SCALAR (and levels 0-1, which have no cluster fit) is the
+ * plain path.  Same arguments and results otherwise as
  * icbc_gpu_compress_bc1_blocks / icbc_gpu_compress_bc1_image, which they
- * replace for that build (icbc.h:48, :3846).  NEON (ICBC_SIMD=-1) is not
- * offered: its vmlaq_f32 / vmlsq_f32 fuse or not with the compiler's
- * contraction setting, so its output is not fixed by the source.
+ * replace for that build (icbc.h:48, :3846).  Values are ICBC_SIMD's.
  * ---------------------------------------------------------------------- */
 enum {
+    ICBC_GPU_SIMD_NEON = -1,  /* 4 lanes, half to even, vsaturate keeps NaN (ICBC_NEON) */
     ICBC_GPU_SIMD_SCALAR = 0, /* ICBC_SIMD=0 (the plain path) */
     ICBC_GPU_SIMD_SSE2 = 1,   /* 4 lanes, vround01 = int(x + 0.5f) */
     ICBC_GPU_SIMD_SSE41 = 2,  /* 4 lanes, half to even */

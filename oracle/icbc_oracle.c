@@ -72,23 +72,30 @@ static const float k_mid6[64] = {
 
 /* SIMD profiles of the reference (ICBC_SIMD, icbc.h:59-66): the vector
  * width of the cluster-fit loops, whether vmadd/vmsub are fused (AVX2 and
- * AVX-512: icbc.h:734-752, :970-980) and whether vround01 rounds half to even
- * (SSE4.1 and later: icbc.h:518-524, :764-766, :988-990) instead of
- * int(x + 0.5f) (scalar, SSE2: icbc.h:417, :522).  Index 0 is the scalar
- * profile; 1..5 are ICBC_SSE2, ICBC_SSE41, ICBC_AVX1, ICBC_AVX2, ICBC_AVX512. */
-typedef struct { int vec, fma, rne; } prof_t;
-static const prof_t k_prof[6] = {{1, 0, 0}, {4, 0, 0}, {4, 0, 1}, {8, 0, 1}, {8, 1, 1}, {16, 1, 1}};
+ * AVX-512: icbc.h:734-752, :970-980), whether vround01 rounds half to even
+ * (SSE4.1 and later, NEON: icbc.h:518-524, :764-766, :988-990, :1159-1162)
+ * instead of int(x + 0.5f) (scalar, SSE2: icbc.h:417, :522), and whether
+ * vsaturate keeps a NaN (NEON: vmaxq_f32 / vminq_f32 return NaN for a NaN
+ * operand, icbc.h:1155-1157; the x86 max/min and the scalar template return
+ * the other operand, so NaN saturates to 0).  Index 0 is the scalar profile;
+ * 1..5 are ICBC_SSE2, ICBC_SSE41, ICBC_AVX1, ICBC_AVX2, ICBC_AVX512; 6 is
+ * ICBC_NEON (ICBC_SIMD=-1) built without FP contraction, where vmlaq_f32 /
+ * vmlsq_f32 are a multiply then an add (icbc.h:1142-1153). */
+typedef struct { int vec, fma, rne, nan; } prof_t;
+static const prof_t k_prof[7] = {{1, 0, 0, 0}, {4, 0, 0, 0}, {4, 0, 1, 0}, {8, 0, 1, 0},
+                                 {8, 1, 1, 0}, {16, 1, 1, 0}, {4, 0, 1, 1}};
 
 static inline float p_madd(const prof_t *p, float a, float b, float c) { return p->fma ? fmaf(a, b, c) : a * b + c; }
 static inline float p_msub(const prof_t *p, float a, float b, float c) { return p->fma ? fmaf(a, b, -c) : a * b - c; }
 /* vm2sub(a, b, c, d) = vmsub(a, b, c * d) (icbc.h:415, :754-756, :978-980). */
 static inline float p_m2sub(const prof_t *p, float a, float b, float c, float d) { return p_msub(p, a, b, c * d); }
 static inline float p_round01(const prof_t *p, float a) { return p->rne ? nearbyintf(a) : (float)(int)(a + 0.5f); }
+static inline float p_saturate(const prof_t *p, float a) { return (p->nan && a != a) ? a : vsaturate(a); }
 static inline v3 p_round_ept(const prof_t *p, v3 v) {
     v3 r;
-    r.x = p_round01(p, vsaturate(v.x) * 31.0f) * (1.0f / 31.0f);
-    r.y = p_round01(p, vsaturate(v.y) * 63.0f) * (1.0f / 63.0f);
-    r.z = p_round01(p, vsaturate(v.z) * 31.0f) * (1.0f / 31.0f);
+    r.x = p_round01(p, p_saturate(p, v.x) * 31.0f) * (1.0f / 31.0f);
+    r.y = p_round01(p, p_saturate(p, v.y) * 63.0f) * (1.0f / 63.0f);
+    r.z = p_round01(p, p_saturate(p, v.z) * 31.0f) * (1.0f / 31.0f);
     return r;
 }
 
@@ -882,7 +889,7 @@ float oracle_compress_bc1(int decoder, int level, const float *in, const float *
                           int three_color_mode, int three_color_black, void *outp, oracle_stats *st) {
     oracle_init();
     int profile = (decoder >> ORACLE_PROFILE_SHIFT) & 7;
-    const prof_t *pf = &k_prof[profile < 6 ? profile : 0];
+    const prof_t *pf = &k_prof[profile < 7 ? profile : 0];
     decoder &= 3;
     const dec_tables *dt = &g_dec[decoder];
     options opt = setup_options(level, three_color_mode, three_color_black);

@@ -29,10 +29,13 @@ enum { ORACLE_D3D10 = 0, ORACLE_NVIDIA = 1, ORACLE_AMD = 2, ORACLE_INTEL = 3 };
  * in bits 8..10: (profile << ORACLE_PROFILE_SHIFT) | decoder.  Profile 0 is
  * the scalar build (ICBC_SIMD=0); 1..5 reproduce the cluster-fit loops of the
  * ICBC_SSE2, ICBC_SSE41, ICBC_AVX1, ICBC_AVX2 and ICBC_AVX512 builds (vector
- * width, lane tie-break, fused vmadd/vmsub, vround01 rounding), each compiled
- * without FP contraction.  Nothing else in the encoder depends on ICBC_SIMD. */
+ * width, lane tie-break, fused vmadd/vmsub, vround01 rounding), and 6 those of
+ * the ICBC_NEON build (ICBC_SIMD=-1: four lanes, half-even rounding, NaN kept
+ * by vsaturate), each compiled without FP contraction.  Nothing else in the
+ * encoder depends on ICBC_SIMD. */
 #define ORACLE_PROFILE_SHIFT 8
-enum { ORACLE_SCALAR = 0, ORACLE_SSE2 = 1, ORACLE_SSE41 = 2, ORACLE_AVX1 = 3, ORACLE_AVX2 = 4, ORACLE_AVX512 = 5 };
+enum { ORACLE_SCALAR = 0, ORACLE_SSE2 = 1, ORACLE_SSE41 = 2, ORACLE_AVX1 = 3, ORACLE_AVX2 = 4, ORACLE_AVX512 = 5,
+       ORACLE_NEON = 6 };
 
 /* Per-block work counters used to derive the algorithmic FP32 operation
  * count of a workload (units of the reference's scalar inner loops). */

@@ -11,8 +11,8 @@ package ``icbc_gb300``.
   ``_ref/libicbc_ref_simd<N>.so`` are its x86 SIMD builds (N = ICBC_SIMD 1..5).
 
 SIMD profiles: every ``decoder`` below may be combined with ``profile``
-(0 scalar, 1 SSE2, 2 SSE4.1, 3 AVX, 4 AVX2, 5 AVX-512); the oracle then
-reproduces that build's cluster-fit loops.
+(0 scalar, 1 SSE2, 2 SSE4.1, 3 AVX, 4 AVX2, 5 AVX-512, 6 NEON); the oracle
+then reproduces that build's cluster-fit loops.
 """
 from __future__ import annotations
 
@@ -32,7 +32,7 @@ _lib = None
 _ref = {}
 
 PROFILE_SHIFT = 8
-PROFILES = {"scalar": 0, "sse2": 1, "sse41": 2, "avx": 3, "avx2": 4, "avx512": 5}
+PROFILES = {"scalar": 0, "sse2": 1, "sse41": 2, "avx": 3, "avx2": 4, "avx512": 5, "neon": 6}
 
 
 def ref_path(profile: int = 0) -> str:

@@ -168,6 +168,39 @@ def test_batch_matches_plain_and_oracle(gpu_lib):
         assert np.array_equal(out.cpu().numpy(), ob)
 
 
+_FIRST_CALL_BATCH = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+import icbc_gb300 as ig
+from icbc_gb300 import synth
+ig.init(ig.Decoder_D3D10)
+imgs = [torch.from_numpy(synth.hard_mixture_image(4096, 4096, 7)).cuda(),
+        torch.from_numpy(synth.gradient_noise_rects(200, 120, 3)).cuda()]
+outs = [[torch.zeros((ig.blocks_of(im.shape[1], im.shape[0]), 8), dtype=torch.uint8, device="cuda")
+         for im in imgs] for _ in range(2)]
+descs = [[ig.image_desc(im, lv, o, None, 0, (1, 1, 1), ig.WEIGHTS_ALPHA) for im, o, lv in zip(imgs, outs[k], (9, 8))]
+         for k in range(2)]
+batch = ig.Batch(descs[0])   # the first encode of the process
+batch.launch()
+ig.compress_images_each(descs[1])
+torch.cuda.synchronize()
+assert all(torch.equal(a, b) for a, b in zip(outs[0], outs[1]))
+print("ok")
+"""
+
+
+def test_batch_as_first_call_of_a_process(gpu_lib):
+    """A batch whose image is large enough (2^20 blocks) for its own kernels
+    takes stream-ordered scratch inside the batch's graph capture; that must
+    work when the batch is the first encode of a process (the scratch pool is
+    created before the capture)."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _FIRST_CALL_BATCH, root], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stderr[-2000:]
+
+
 def test_batch_level9_refinement_pass(gpu_lib):
     """Level-9 images of a batch refine in a second launch whose lanes serve
     blocks of different images: each image's decoder, flags, colour weights

@@ -126,6 +126,30 @@ def test_oracle_simd_profiles_match_golden(profile):
                     assert np.array_equal(e.view(np.uint32), g[key + "_errors"].view(np.uint32)), key
 
 
+def test_oracle_neon_profile():
+    """The NEON profile (ICBC_SIMD=-1 without FP contraction) runs the SSE4.1
+    build's arithmetic -- four lanes, half-even vround01, unfused vmadd --
+    except that vsaturate keeps a NaN.  No NaN reaches a winning combination
+    on ordinary blocks, so there it must give the SSE4.1 build's golden
+    output; blocks with weights spread over 1e-30..1e30 make degenerate
+    combinations NaN, and there the two profiles must part on some blocks."""
+    g = np.load(os.path.join(GOLDEN, "simd.npz"))
+    neon = O.PROFILES["neon"]
+    for si in range(2):
+        cols, wt, cw = g["set%d_colors" % si], g["set%d_weights" % si], tuple(g["set%d_cw" % si])
+        for lvl in SIMD_LEVELS:
+            for dec in range(4):
+                for tc, tcb in SIMD_FLAGS:
+                    key = "set%d_P2_L%d_D%d_tc%d_tcb%d" % (si, lvl, dec, tc, tcb)
+                    b, e = O.compress_blocks(cols, wt, lvl, dec, cw, tc, tcb, profile=neon)
+                    assert np.array_equal(b, g[key + "_blocks"]), key
+                    assert np.array_equal(e.view(np.uint32), g[key + "_errors"].view(np.uint32)), key
+    cols, w = synth.extreme_weight_blocks(4000, seed=5)
+    a, _ = O.compress_blocks(cols, w, 8, 0, (1, 1, 1), True, True, nthreads=8, profile=O.PROFILES["sse41"])
+    b, _ = O.compress_blocks(cols, w, 8, 0, (1, 1, 1), True, True, nthreads=8, profile=neon)
+    assert 0 < (a != b).any(1).sum() < 4000
+
+
 @pytest.mark.parametrize("profile", range(1, 6))
 def test_oracle_simd_profiles_match_compiled_builds(profile):
     """The same against the SIMD builds themselves on other blocks (x86 hosts
