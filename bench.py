@@ -308,6 +308,10 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     ig.init(ig.Decoder_D3D10)
     sms = ig.load().icbc_gpu_sm_count()
+    if args.cta_warps:
+        for lv in range(2, 10):
+            g, p, _ = ig.get_launch_config(lv)
+            ig.set_launch_config(lv, g, p, args.cta_warps)
     if args.only_hard:  # profiling runs of the hard-mixture leg alone
         peak = fp32_peak_tops(load_peaks(), sms)
         print(json.dumps({"hard": hard_leg(ig, torch, dev, args, peak), "profiling_run": True}))
@@ -330,8 +334,10 @@ def run_ours(args):
     tuning = None
     if not args.no_autotune:
         table = ig.autotune(d_img, LEVELS, color_weights=CW, weight_mode=ig.WEIGHTS_ALPHA)
-        tuning = {str(lv): "%d groups/warp, %s" % (t["groups_per_warp"], "persistent" if t["persistent"] else
-                                                    "hw-balanced") for lv, t in table.items()}
+        tuning = {str(lv): "%d groups/warp, %s%s" % (t["groups_per_warp"], "persistent" if t["persistent"] else
+                                                      "hw-balanced",
+                                                      ", listed pass %d-warp CTAs" % t["cta_warps"] if lv >= 2 else "")
+                  for lv, t in table.items()}
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -736,6 +742,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-hard", action="store_true", help="skip the hard-distribution leg")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--cta-warps", type=int, default=0, choices=[0, 4, 8, 16],
+                    help="the listed pass's CTA size at levels 2-9 (the autotuner, unless off, may change it)")
     ap.add_argument("--hard-images", type=int, default=64)
     ap.add_argument("--hard-side", type=int, default=8192)
     ap.add_argument("--hard-steps", type=int, default=2)

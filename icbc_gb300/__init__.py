@@ -55,7 +55,7 @@ class ImageDesc(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     """struct icbc_gpu_launch_config."""
-    _fields_ = [("groups_per_warp", ctypes.c_int32), ("persistent", ctypes.c_int32)]
+    _fields_ = [("groups_per_warp", ctypes.c_int32), ("persistent", ctypes.c_int32), ("cta_warps", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -622,28 +622,39 @@ class Server:
 
 # ---------------------------------------------------------------- autotuner
 
+# Launch shapes the autotuner tries: (groups_per_warp, persistent) for the
+# kernels that take one block per lane (levels 0-1, the first pass of levels
+# 2-9), and the CTA size of the pass that encodes the listed blocks of
+# levels 2-9 (4: warp-wide searches; 8, 16: CTA-wide).
 TUNE_CANDIDATES = [(g, p) for p in (0, 1) for g in (1, 2, 4, 8)]
+TUNE_CTA_WARPS = (4, 8, 16)
 
 
-def get_launch_config(level: int) -> tuple[int, int]:
+def get_launch_config(level: int) -> tuple[int, int, int]:
+    """(groups_per_warp, persistent, cta_warps) of a level (cta_warps 0: the level's default)."""
     c = LaunchConfig()
     _check(load().icbc_gpu_get_launch_config(int(level), ctypes.byref(c)), "get_launch_config")
-    return c.groups_per_warp, c.persistent
+    return c.groups_per_warp, c.persistent, c.cta_warps
 
 
-def set_launch_config(level: int, groups_per_warp: int, persistent: int) -> None:
-    c = LaunchConfig(int(groups_per_warp), int(persistent))
+def set_launch_config(level: int, groups_per_warp: int, persistent: int, cta_warps: int | None = None) -> None:
+    """Sets a level's launch shape; cta_warps None keeps the current one."""
+    if cta_warps is None:
+        cta_warps = get_launch_config(level)[2]
+    c = LaunchConfig(int(groups_per_warp), int(persistent), int(cta_warps))
     _check(load().icbc_gpu_set_launch_config(int(level), ctypes.byref(c)), "set_launch_config")
 
 
-def autotune(image, levels=range(10), candidates=TUNE_CANDIDATES, repeats: int = 3, decoder: int = Decoder_D3D10,
-             color_weights=(1.0, 1.0, 1.0), weight_mode: int = WEIGHTS_UNIFORM, apply: bool = True,
-             path: str | None = None) -> dict:
-    """Times every launch shape of the plain image kernel on `image` (a CUDA
-    uint8 tensor (h, w, 4)) for each level with CUDA events, keeps the fastest
-    (applied to the library when `apply`), and returns
-    {level: {"groups_per_warp", "persistent", "ms", "candidates": {...}}}.
-    With `path` the table is also written as JSON (load_tuning reads it)."""
+def autotune(image, levels=range(10), candidates=TUNE_CANDIDATES, cta_candidates=TUNE_CTA_WARPS, repeats: int = 3,
+             decoder: int = Decoder_D3D10, color_weights=(1.0, 1.0, 1.0), weight_mode: int = WEIGHTS_UNIFORM,
+             apply: bool = True, path: str | None = None) -> dict:
+    """Times launch shapes of the plain image kernels on `image` (a CUDA
+    uint8 tensor (h, w, 4)) for each level with CUDA events and keeps the
+    fastest (applied to the library when `apply`): first (groups_per_warp,
+    persistent) over `candidates`, then, at levels 2-9, the listed pass's CTA
+    size over `cta_candidates`.  Returns {level: {"groups_per_warp",
+    "persistent", "cta_warps", "ms", "candidates": {...}}}.  With `path` the
+    table is also written as JSON (load_tuning reads it)."""
     import json
     torch = _torch()
     nb = blocks_of(int(image.shape[1]), int(image.shape[0]))
@@ -651,25 +662,39 @@ def autotune(image, levels=range(10), candidates=TUNE_CANDIDATES, repeats: int =
     stream.wait_stream(torch.cuda.current_stream())  # the image is ready
     with torch.cuda.stream(stream):
         out = torch.zeros((nb, 8), dtype=torch.uint8, device=image.device)
+
+    def timed():
+        with torch.cuda.stream(stream):
+            compress_image(image, lv, decoder, color_weights, weight_mode, out=out, stream=stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(repeats):
+                compress_image(image, lv, decoder, color_weights, weight_mode, out=out, stream=stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / repeats
+
     table = {}
     for lv in levels:
         before = get_launch_config(lv)
         times = {}
         for g, p in candidates:
-            set_launch_config(lv, g, p)
-            with torch.cuda.stream(stream):
-                compress_image(image, lv, decoder, color_weights, weight_mode, out=out, stream=stream)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                for _ in range(repeats):
-                    compress_image(image, lv, decoder, color_weights, weight_mode, out=out, stream=stream)
-                e1.record(stream)
-            torch.cuda.synchronize()
-            times["%d/%d" % (g, p)] = e0.elapsed_time(e1) / repeats
+            set_launch_config(lv, g, p, before[2])
+            times["%d/%d" % (g, p)] = timed()
         best = min(times, key=times.get)
         g, p = (int(x) for x in best.split("/"))
-        set_launch_config(lv, *((g, p) if apply else before))
-        table[int(lv)] = {"groups_per_warp": g, "persistent": p, "ms": times[best], "candidates": times}
+        cta = before[2]
+        if lv >= 2 and cta_candidates:
+            ctimes = {}
+            for c in cta_candidates:
+                set_launch_config(lv, g, p, c)
+                ctimes[c] = timed()
+                times["%d/%d/cta%d" % (g, p, c)] = ctimes[c]
+            cta = min(ctimes, key=ctimes.get)
+            best = "%d/%d/cta%d" % (g, p, cta)
+        set_launch_config(lv, *((g, p, cta) if apply else before))
+        table[int(lv)] = {"groups_per_warp": g, "persistent": p, "cta_warps": cta, "ms": times[best],
+                          "candidates": times}
     if path:
         with open(path, "w") as f:
             json.dump({str(k): v for k, v in table.items()}, f, indent=1)
@@ -682,4 +707,4 @@ def load_tuning(path: str) -> None:
     with open(path) as f:
         table = json.load(f)
     for lv, cfg in table.items():
-        set_launch_config(int(lv), cfg["groups_per_warp"], cfg["persistent"])
+        set_launch_config(int(lv), cfg["groups_per_warp"], cfg["persistent"], cfg.get("cta_warps", 0))

@@ -21,7 +21,7 @@
 //                   of their rows, or to different entries of any rows in
 //                   the cluster search, spread over the 8 bank groups)
 //   slots [32]      u64 per block: best (error, table index) of a cluster search
-//   info  [32]      int per block: its first combination | colour count << 16
+//   info  [32]      int per block: its first combination | colour count << 24
 // 17 KB per warp: three 4-warp CTAs per SM at levels 2..9.
 #pragma once
 
@@ -86,7 +86,7 @@ struct WarpCtx {
     float *in;
     float *sat;                  // per block: 17 float4 (r, g, b, w) SAT entries
     unsigned long long *slots;   // per block: the search's argmin key
-    int *info;                   // per block: first combination | count << 16
+    int *info;                   // per block: first combination | count << 24
     int lane;
 };
 
@@ -699,6 +699,10 @@ struct Walker {
     int best_k;
 };
 
+// A block's search info word: its first combination in the group's list
+// (bits 0-23) and its colour count (bits 24-28; 0: no search).
+constexpr int kInfoShift = 24;
+constexpr int kInfoMask = (1 << kInfoShift) - 1;
 __device__ __forceinline__ int block_info(const WarpCtx &w, int b) { return w.info[b]; }
 
 // With SIMD, a block's combinations run to a whole number of vectors of
@@ -709,7 +713,7 @@ __device__ __forceinline__ int padded_total(int t, int vec) { return (t + vec - 
 template <bool FOUR, bool SIMD = false>
 __device__ __forceinline__ void walker_enter(const WarpCtx &w, Walker &v, int b, int k, int vec = 1) {
     const float *S = w.sat + b * kSatStride;
-    const int cnt = w.info[b] >> 16;
+    const int cnt = w.info[b] >> kInfoShift;
     v.b = b;
     v.k = k;
     v.S = S;
@@ -729,9 +733,10 @@ __device__ __forceinline__ void walker_flush(const WarpCtx &w, const Walker &v) 
     }
 }
 
-// Starts a walker at global combination g (if any work is left for it).
-template <bool FOUR, bool SIMD = false>
-__device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g, int gend, int vec = 1) {
+// Starts a walker at global combination g (if any work is left for it),
+// over a search group of NB blocks.
+template <bool FOUR, int NB, bool SIMD = false>
+__device__ __forceinline__ void walker_start_n(const WarpCtx &w, Walker &v, int g, int gend, int vec = 1) {
     v.g = g;
     v.gend = gend;
     v.S = w.sat;
@@ -743,14 +748,19 @@ __device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g,
     v.b = 0;
     if (g < gend) {
         // The last block whose first combination is <= g always has work.
-        int lo = 0, hi = 32;
+        int lo = 0, hi = NB;
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if ((block_info(w, mid) & 0xffff) <= g) lo = mid;
+            if ((block_info(w, mid) & kInfoMask) <= g) lo = mid;
             else hi = mid;
         }
-        walker_enter<FOUR, SIMD>(w, v, lo, g - (block_info(w, lo) & 0xffff), vec);
+        walker_enter<FOUR, SIMD>(w, v, lo, g - (block_info(w, lo) & kInfoMask), vec);
     }
+}
+
+template <bool FOUR, bool SIMD = false>
+__device__ __forceinline__ void walker_start(const WarpCtx &w, Walker &v, int g, int gend, int vec = 1) {
+    walker_start_n<FOUR, 32, SIMD>(w, v, g, gend, vec);
 }
 
 // One step: fold the error of combination k in, move to k + 1, and cross
@@ -788,7 +798,7 @@ template <bool FOUR, bool SIMD = false>
 __device__ __forceinline__ void walker_cross(const WarpCtx &w, Walker &v, uint32_t &next, int vec = 1) {
     walker_flush(w, v);
     int nb = v.b + 1;
-    while ((block_info(w, nb) >> 16) == 0) nb++;
+    while ((block_info(w, nb) >> kInfoShift) == 0) nb++;
     walker_enter<FOUR, SIMD>(w, v, nb, 0, vec);
     next = (FOUR ? w.T->four : w.T->three)[0];
 }
@@ -809,7 +819,7 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
         if (lane >= off) incl += y;
     }
     const int W = __shfl_sync(kFull, incl, 31);
-    w.info[lane] = (incl - T) | ((need ? count : 0) << 16);
+    w.info[lane] = (incl - T) | ((need ? count : 0) << kInfoShift);
     w.slots[lane] = ~0ull;
     __syncwarp();
     if (W == 0) return -1;
@@ -854,6 +864,68 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
     const unsigned long long key = w.slots[lane];
     if (!need || key == ~0ull) return -1;
     return SIMD ? simd_unrank((int)(uint32_t)key, vec) : (int)(uint32_t)key;
+}
+
+// The same search over a group of NW warps (the whole CTA): the combinations
+// of the group's 32 * NW blocks form one list cut into 64 * NW equal ranges,
+// two per thread.  `g` is the group's context: its sat / info / slots hold
+// the rows of all the group's blocks, block j = warp * 32 + lane, and
+// g.lane = threadIdx.x.  `sums` is NW ints of shared memory.  Every thread of
+// the CTA must call it together (it synchronises the CTA) with the same fit
+// weights `q`: every thread walks combinations of any of the group's blocks.
+// Same winner rule as flat_search: per block the smallest (error, table index).
+template <bool FOUR, int NW>
+__device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bool need, int count,
+                                                 const FitWeights &q) {
+    const int j = threadIdx.x;
+    const int lane = j & 31, warp = j >> 5;
+    const int T = need ? (FOUR ? g.T->four_total[count - 1] : g.T->three_total[count - 1]) : 0;
+    int incl = T;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) sums[warp] = incl;
+    __syncthreads();
+    int before = 0, W = 0;
+#pragma unroll
+    for (int k = 0; k < NW; k++) {
+        const int v = sums[k];
+        before += k < warp ? v : 0;
+        W += v;
+    }
+    g.info[j] = (before + incl - T) | ((need ? count : 0) << kInfoShift);
+    g.slots[j] = ~0ull;
+    __syncthreads();
+    if (W == 0) return -1;
+    const int per = (W + 64 * NW - 1) / (64 * NW);
+    Walker A, B;
+    walker_start_n<FOUR, 32 * NW>(g, A, min(j * per, W), min(j * per + per, W));
+    walker_start_n<FOUR, 32 * NW>(g, B, min((j + 32 * NW) * per, W), min((j + 32 * NW) * per + per, W));
+    const uint32_t *table = FOUR ? g.T->four : g.T->three;
+    uint32_t pa = table[A.k], pb = table[B.k];
+    for (int it = 0; it < per; it++) {
+        uint32_t na = table[A.k + 1], nb = table[B.k + 1];
+        V3 a, b;
+        const float ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
+        const float eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
+        walker_fold(A, ea);
+        walker_fold(B, eb);
+        const bool xa = walker_crossing(A), xb = walker_crossing(B);
+        if (__any_sync(kFull, xa || xb)) {
+            if (xa) walker_cross<FOUR>(g, A, na);
+            if (xb) walker_cross<FOUR>(g, B, nb);
+        }
+        pa = na;
+        pb = nb;
+    }
+    walker_flush(g, A);
+    walker_flush(g, B);
+    __syncthreads();
+    const unsigned long long key = g.slots[j];
+    if (!need || key == ~0ull) return -1;
+    return (int)(uint32_t)key;
 }
 
 // ------------------------------------------------------------- encoder --
@@ -928,9 +1000,16 @@ __device__ __forceinline__ float trivial_block(const DecoderTables *D, const flo
     return block_error<UNROLL>(row, p.cw, palette_f(c0, c1, p.decoder, lut255, D), idx);
 }
 
-template <int L, bool DEFER, bool SIMD = false, class Row>
+// With NW > 1 the cluster searches run over the whole CTA of NW warps
+// (flat_search_group on the group context *g, NW ints of shared memory at
+// gsums): every thread of the CTA must make the call together.  The group
+// search shares one set of fit weights, so it needs every thread's decoder
+// and colour weights alike; `group` false (the same for the whole CTA) makes
+// each warp search its own blocks instead.
+template <int L, bool DEFER, bool SIMD = false, int NW = 1, class Row>
 __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row, const EncodeParams &p, bool active,
-                                                uint32_t &c0, uint32_t &c1, uint32_t &idx, bool &refine_next) {
+                                                uint32_t &c0, uint32_t &c1, uint32_t &idx, bool &refine_next,
+                                                const WarpCtx *g = nullptr, int *gsums = nullptr, bool group = true) {
     using O = Level<L>;
     refine_next = false;
     const int lane = w.lane;
@@ -970,7 +1049,9 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         __syncwarp();
         // 4-colour cluster fit of every block that needs one, across the warp.
         const FitWeights q = fit_weights(w.D, metric);
-        const int my4 = flat_search<true, SIMD>(w, need4, count, q, &p);
+        int my4;
+        if (NW > 1 && group) my4 = flat_search_group<true, NW>(*g, gsums, need4, count, q);
+        else my4 = flat_search<true, SIMD>(w, need4, count, q, &p);
         uint32_t f0 = 0, f1 = 0, fi = 0;
         float ferr = 0.0f;
         bool need3 = false;
@@ -1002,7 +1083,9 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
             }
         }
         __syncwarp();
-        const int my3 = flat_search<false, SIMD>(w, need3, count3, q, &p);
+        int my3;
+        if (NW > 1 && group) my3 = flat_search_group<false, NW>(*g, gsums, need3, count3, q);
+        else my3 = flat_search<false, SIMD>(w, need3, count3, q, &p);
         if (need3) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
             if (my3 >= 0) {

@@ -164,6 +164,7 @@ cudaError_t launch_simd(const GlobalTables *G, const ImageDesc *image, const Blo
 struct LaunchShape {
     int groups_per_warp;
     bool persistent;
+    int cta_warps;  // the listed pass's CTA size (0: the level's default)
 };
 LaunchShape launch_shape(int level);
 

@@ -5,6 +5,8 @@
 // add separately rounded, as the reference's scalar build does.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "bc1_batch_task.cuh"
 
 #ifndef ICBC_LEVEL
@@ -219,6 +221,181 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_listed(const Glo
 // run_batch with the level fixed, so the kernel holds one level's code as the
 // plain kernels do (the all-levels kernel stalls about twice as often on
 // instruction fetch for the same blocks).
+// k_image_listed with the CTA as the unit: NW warps take 32 * NW listed
+// blocks at a time and move through the encoder's stages together -- colour
+// reduction and summed-area tables one block per lane, then the cluster
+// searches over all the CTA's blocks at once (flat_search_group), then the
+// output blocks.  All warps of an SM run the same stage's code at the same
+// time, and a search balances over 32 * NW blocks instead of 32.  Same
+// arithmetic and the same winner per block as k_image_listed.  Shared memory:
+// the tables, then the CTA's byte rows, SAT rows, argmin slots, info words
+// and NW scan sums (group_smem_bytes).
+template <int NW>
+__host__ __device__ constexpr size_t group_smem_bytes() {
+    return sizeof(SharedTables) + (size_t)NW * 32 * (kInWordsByte * 4 + kSatStride * 4 + 8 + 4) + NW * 4;
+}
+
+// The batched CTA-wide kernel's layout: the group layout (16-byte aligned
+// size), NW 16-byte round keys and the round's first task.
+template <int NW>
+__host__ __device__ constexpr size_t batch_smem_bytes() {
+    return group_smem_bytes<NW>() + NW * 16 + 16;
+}
+static_assert(group_smem_bytes<8>() % 16 == 0 && group_smem_bytes<16>() % 16 == 0, "round keys need 16-byte alignment");
+
+// The warp's and the CTA's contexts in the group layout, and the scan sums.
+template <int NW>
+__device__ __forceinline__ void group_ctx(unsigned char *smem, const SharedTables &T, const DecoderTables *D,
+                                          WarpCtx &w, WarpCtx &g, int *&sums) {
+    uint32_t *in = reinterpret_cast<uint32_t *>(smem + sizeof(SharedTables));
+    float *sat = reinterpret_cast<float *>(in + NW * 32 * kInWordsByte);
+    unsigned long long *slots = reinterpret_cast<unsigned long long *>(sat + NW * 32 * kSatStride);
+    int *info = reinterpret_cast<int *>(slots + NW * 32);
+    sums = info + NW * 32;
+    const int warp = threadIdx.x >> 5;
+    g.T = &T;
+    g.D = D;
+    g.in = reinterpret_cast<float *>(in);
+    g.sat = sat;
+    g.slots = slots;
+    g.info = info;
+    g.lane = threadIdx.x;
+    w = g;
+    w.in = reinterpret_cast<float *>(in + warp * 32 * kInWordsByte);
+    w.sat = sat + warp * 32 * kSatStride;
+    w.slots = slots + warp * 32;
+    w.info = info + warp * 32;
+    w.lane = threadIdx.x & 31;
+}
+
+template <int L, bool DEFER, int NW>
+__global__ void __launch_bounds__(NW * 32, 512 / (NW * 32))
+    k_image_listed_cta(const GlobalTables *G, ImageDesc d, EncodeParams p, const uint32_t *list,
+                       const unsigned int *listed, RefineSlot *st) {
+    const int64_t n = *listed;
+    const int64_t groups = (n + 32 * NW - 1) / (32 * NW);
+    if ((int64_t)blockIdx.x >= groups) return;  // the whole CTA has no work
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    WarpCtx w, g;
+    int *sums;
+    group_ctx<NW>(smem, T, &G->dec[p.decoder], w, g, sums);
+    uint32_t *in = reinterpret_cast<uint32_t *>(g.in);
+    const ByteRow row = byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA);
+    for (int64_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+        const int64_t k = grp * (32 * NW) + threadIdx.x;
+        const bool active = k < n;
+        const int64_t b = active ? (int64_t)list[k] : 0;
+        __syncwarp();
+        if (active) load_image_block_bytes(d, b, in + threadIdx.x * kInWordsByte);
+        __syncwarp();
+        uint32_t c0 = 0, c1 = 0, idx = 0;
+        if (L >= 4 && active) {
+            const uint2 prev = d.out[b];
+            c0 = prev.x & 0xffff;
+            c1 = prev.x >> 16;
+            idx = prev.y;
+        }
+        bool pending;
+        const float e = encode_warp_ex<L, DEFER, false, NW>(w, row, p, active, c0, c1, idx, pending, &g, sums);
+        if (active) {
+            d.out[b] = make_uint2(c0 | (c1 << 16), idx);
+            if (d.errors) d.errors[b] = e;
+            if (DEFER) st[b] = RefineSlot{e, pending ? 1u : 0u};
+        }
+    }
+}
+
+// k_batch_level with the CTA as the unit: the CTA takes NW tasks at a time
+// (one per warp; past the end of the queue a warp has no blocks, but its
+// threads still walk the round's combinations) and moves through the
+// encoder's stages together, the cluster searches over all its blocks at
+// once -- when every task of the round has the same decoder and colour
+// weights (every walker must use the same fit weights); otherwise each warp
+// searches its own blocks that round.  Levels 2-9 of a byte-row batch; at
+// level 9 every image refines in k_refine's batch mode (the planner gives
+// each level-9 image of the shared kernel a slot range).
+template <int LV, int NW>
+__global__ void __launch_bounds__(NW * 32, 512 / (NW * 32))
+    k_batch_level_cta(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int task0, int ntasks,
+                      int *counter, const int64_t *refine_base, RefineSlot *slots, BatchLists lists) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    SharedTables &T = *reinterpret_cast<SharedTables *>(smem);
+    stage_tables(T, G);
+    WarpCtx w, g;
+    int *sums;
+    group_ctx<NW>(smem, T, &G->dec[0], w, g, sums);
+    // Round state past the group layout: each warp's (decoder, colour
+    // weights), then the CTA's first task (batch_smem_bytes).
+    uint4 *warp_key = reinterpret_cast<uint4 *>(smem + group_smem_bytes<NW>());
+    int *round_task = reinterpret_cast<int *>(warp_key + NW);
+    uint32_t *in = reinterpret_cast<uint32_t *>(g.in);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        if (threadIdx.x == 0) *round_task = atomicAdd(counter, NW);
+        __syncthreads();
+        const int t = *round_task + warp;
+        if (t - warp >= ntasks) break;
+        const bool has_task = t < ntasks;
+        const BatchTask task = has_task ? tasks[task0 + t] : BatchTask{0u, 0u};
+        const ImageDesc &d = images[task.image];
+        const int64_t lb = lists.list ? lists.list_base[task.image] : -1;
+        int64_t b = (int64_t)task.first_block + lane;
+        bool active = has_task && b < d.nblocks;
+        if (has_task && lb >= 0) {
+            const int64_t n = lists.listed[task.image];
+            active = b < n;  // tasks past the list's end: finished by the first pass
+            b = active ? (int64_t)lists.list[lb + b] : 0;
+        }
+        if (lane == 0)
+            warp_key[warp] = has_task ? make_uint4((uint32_t)d.decoder, __float_as_uint(d.cw[0]),
+                                                   __float_as_uint(d.cw[1]), __float_as_uint(d.cw[2]))
+                                      : make_uint4(0xffffffffu, 0u, 0u, 0u);
+        __syncthreads();
+        // One search over the CTA when every warp with a task has the same key.
+        bool group = true;
+        uint4 first = make_uint4(0xffffffffu, 0u, 0u, 0u);
+#pragma unroll
+        for (int k = 0; k < NW; k++) {
+            const uint4 v = warp_key[k];
+            if (v.x == 0xffffffffu) continue;
+            if (first.x == 0xffffffffu) first = v;
+            group &= v.x == first.x && v.y == first.y && v.z == first.z && v.w == first.w;
+        }
+        // Every thread walks the group's combinations with its own fit
+        // weights, so a warp without a task takes the round's (decoder,
+        // colour weights); warp 0 always has a task.
+        EncodeParams p;
+        p.decoder = has_task ? d.decoder : (int)first.x;
+        p.three_color_mode = d.three_color_mode;
+        p.three_color_black = d.three_color_black;
+        p.cw = has_task ? v3(d.cw[0], d.cw[1], d.cw[2])
+                        : v3(__uint_as_float(first.y), __uint_as_float(first.z), __uint_as_float(first.w));
+        w.D = &G->dec[p.decoder];
+        const ByteRow row = byte_row(w, d.weight_mode == ICBC_GPU_WEIGHTS_ALPHA);
+        __syncwarp();
+        if (active) load_image_block_bytes(d, b, in + threadIdx.x * kInWordsByte);
+        __syncwarp();
+        uint32_t c0 = 0, c1 = 0, idx = 0;
+        if (LV >= 4 && active) {
+            const uint2 prev = d.out[b];
+            c0 = prev.x & 0xffff;
+            c1 = prev.x >> 16;
+            idx = prev.y;
+        }
+        bool pending = false;
+        const float e = encode_warp_ex<LV, LV == 9, false, NW>(w, row, p, active, c0, c1, idx, pending, &g, sums,
+                                                                group);
+        if (active) {
+            d.out[b] = make_uint2(c0 | (c1 << 16), idx);
+            if (d.errors) d.errors[b] = e;
+            if (LV == 9) slots[refine_base[task.image] + b] = RefineSlot{e, pending ? 1u : 0u};
+        }
+        __syncthreads();  // round_task and warp_key are rewritten next round
+    }
+}
+
 template <int LV>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
     k_batch_level(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks, int task0, int ntasks,
@@ -308,7 +485,38 @@ static int g_resident_blocks = 0, g_resident_image = 0, g_resident_bytes = 0;
 // alpha); weight planes need float rows.
 static bool use_byte_rows(const ImageDesc &d) { return Level<L>::cluster && d.weight_mode != ICBC_GPU_WEIGHTS_PLANE; }
 
-static int g_resident_trivial = 0, g_resident_listed = 0;
+static int g_resident_trivial = 0, g_resident_listed = 0, g_resident_listed8 = 0, g_resident_listed16 = 0;
+static int g_resident_batch8 = 0, g_resident_batch16 = 0;
+
+// The listed pass's CTA size at this level: the launch shape's, else the
+// level's default -- 16-warp CTAs from level 4 on, 4 at levels 2-3, whose
+// short lists gain nothing from CTA-wide searches.
+static int listed_cta_warps() {
+    const int c = launch_shape(L).cta_warps;
+    if (c == 4 || c == 8 || c == 16) return c;
+    return L >= 4 ? 16 : 4;
+}
+
+// The CTA size for an image of `nblocks` blocks: a CTA-wide pass takes
+// 32 * cta_warps listed blocks per CTA, so an image with fewer blocks than
+// two such rounds over every SM would run on a fraction of the SMs; it takes
+// 4-warp CTAs instead.
+static int listed_cta_warps(int64_t nblocks, int sms) {
+    const int c = listed_cta_warps();
+    return c > 4 && nblocks >= (int64_t)sms * 32 * c * 2 ? c : 4;
+}
+
+// Shared-memory limit of a listed-pass kernel and, once, its resident CTAs per SM.
+template <class K>
+static cudaError_t listed_attributes(K kernel, int warps, size_t smem, int *resident) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && !*resident) {
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, warps * 32, smem);
+        *resident = per_sm > 0 ? per_sm : 1;
+    }
+    return e;
+}
 
 // The two passes of kCompact levels, with the list (and at level 9 the
 // refinement hand-over, unless the caller gives one) in stream-ordered
@@ -316,14 +524,15 @@ static int g_resident_trivial = 0, g_resident_listed = 0;
 static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc &d, const EncodeParams &p,
                                           cudaStream_t stream, int sms, RefineSlot *ext_st,
                                           unsigned long long *ext_counter) {
-    const size_t smem = smem_bytes_byte_rows();
-    cudaError_t e =
-        cudaFuncSetAttribute(k_image_listed<L, kDefer>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess && !g_resident_listed) {
-        int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_image_listed<L, kDefer>, kWarpsPerCta * 32, smem);
-        g_resident_listed = per_sm > 0 ? per_sm : 1;
-    }
+    const int cta_warps = listed_cta_warps(d.nblocks, sms);
+    const size_t smem = cta_warps == 16 ? group_smem_bytes<16>()
+                        : cta_warps == 8 ? group_smem_bytes<8>()
+                                         : smem_bytes_byte_rows();
+    cudaError_t e = cudaSuccess;
+    int *resident = cta_warps == 16 ? &g_resident_listed16 : cta_warps == 8 ? &g_resident_listed8 : &g_resident_listed;
+    if (cta_warps == 16) e = listed_attributes(k_image_listed_cta<L, kDefer, 16>, 16, smem, resident);
+    else if (cta_warps == 8) e = listed_attributes(k_image_listed_cta<L, kDefer, 8>, 8, smem, resident);
+    else e = listed_attributes(k_image_listed<L, kDefer>, kWarpsPerCta, smem, resident);
     if (e != cudaSuccess) return e;
     const size_t list_bytes = ((size_t)d.nblocks * 4 + 15) / 16 * 16;
     const size_t slot_bytes = (kDefer && !ext_st) ? ((size_t)d.nblocks * sizeof(RefineSlot) + 15) / 16 * 16 + 16 : 0;
@@ -348,10 +557,16 @@ static cudaError_t launch_image_compacted(const GlobalTables *G, const ImageDesc
     }
     if (e == cudaSuccess) {
         // Persistent over the list, whose length only the device knows.
-        const int64_t most = ((int64_t)d.nblocks + 32 * kWarpsPerCta - 1) / (32 * kWarpsPerCta);
-        const int64_t cap = (int64_t)sms * g_resident_listed;
+        const int per_cta = 32 * (cta_warps == 4 ? kWarpsPerCta : cta_warps);
+        const int64_t most = ((int64_t)d.nblocks + per_cta - 1) / per_cta;
+        const int64_t cap = (int64_t)sms * *resident;
         const int grid = (int)(most < cap ? most : cap);
-        k_image_listed<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed, st);
+        if (cta_warps == 16)
+            k_image_listed_cta<L, kDefer, 16><<<grid, 16 * 32, smem, stream>>>(G, d, p, list, listed, st);
+        else if (cta_warps == 8)
+            k_image_listed_cta<L, kDefer, 8><<<grid, 8 * 32, smem, stream>>>(G, d, p, list, listed, st);
+        else
+            k_image_listed<L, kDefer><<<grid, kWarpsPerCta * 32, smem, stream>>>(G, d, p, list, listed, st);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && kDefer) e = launch_refine(G, &d, nullptr, p, d.out, d.errors, st, d.nblocks, counter, stream, sms);
@@ -395,6 +610,24 @@ cudaError_t ICBC_CAT(launch_batch_level_l, ICBC_LEVEL)(const GlobalTables *G, co
                                                         const BatchTask *tasks, int task0, int ntasks, int *counter,
                                                         cudaStream_t stream, int grid, const int64_t *refine_base,
                                                         RefineSlot *slots, BatchLists lists) {
+    // `grid` counts 4-warp CTAs; a CTA-wide kernel gets as many warps in all.
+    const int cta_warps = Level<L>::cluster && (L < 9 || refine_base) ? listed_cta_warps() : 4;
+    if (cta_warps != 4) {
+        const size_t smem = cta_warps == 16 ? batch_smem_bytes<16>() : batch_smem_bytes<8>();
+        int *resident = cta_warps == 16 ? &g_resident_batch16 : &g_resident_batch8;
+        cudaError_t e = cta_warps == 16 ? listed_attributes(k_batch_level_cta<L, 16>, 16, smem, resident)
+                                        : listed_attributes(k_batch_level_cta<L, 8>, 8, smem, resident);
+        if (e != cudaSuccess) return e;
+        const int want = (grid * kWarpsPerCta + cta_warps - 1) / cta_warps;
+        const int ctas = std::max(1, std::min(want, current_sm_count() * *resident));
+        if (cta_warps == 16)
+            k_batch_level_cta<L, 16><<<ctas, 16 * 32, smem, stream>>>(G, images, tasks, task0, ntasks, counter,
+                                                                       refine_base, slots, lists);
+        else
+            k_batch_level_cta<L, 8><<<ctas, 8 * 32, smem, stream>>>(G, images, tasks, task0, ntasks, counter,
+                                                                     refine_base, slots, lists);
+        return cudaGetLastError();
+    }
     const size_t smem = smem_bytes_byte_rows();
     cudaError_t e = cudaFuncSetAttribute(k_batch_level<L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -348,11 +348,20 @@ int icbc_gpu_compress_bc1_mips(const icbc_gpu_image *image, int32_t levels, void
  * autotuner (icbc_gb300.autotune) or set by hand.  groups_per_warp: groups
  * of 32 blocks each warp takes (1..64); persistent: 1 = exactly the
  * resident CTAs, striding over the image, 0 = enough CTAs for the work,
- * balanced by the hardware.  Defaults: 1 / persistent at levels 0-1,
- * 2 / not persistent at levels 2-9.  Not for use while launches run. */
+ * balanced by the hardware.  cta_warps (levels 2-9, RGBA8 images with
+ * uniform or alpha weights, and the batched form's per-level kernels: the
+ * pass that encodes the blocks of two or more colours): 4 = CTAs of 4 warps,
+ * each warp searching its own 32 blocks' cluster combinations; 8 or 16 =
+ * CTAs of that many warps moving through the encoder's stages together, the
+ * combinations of all the CTA's blocks searched by all its threads (an image
+ * too small for two rounds of such CTAs on every SM takes 4); 0 = the
+ * level's default.  Defaults: 1 / persistent at levels 0-1, 2 / not
+ * persistent at levels 2-9, cta_warps per level.  Not for use while launches
+ * run. */
 typedef struct icbc_gpu_launch_config {
     int32_t groups_per_warp;
     int32_t persistent;
+    int32_t cta_warps;
 } icbc_gpu_launch_config;
 int icbc_gpu_set_launch_config(int level, const icbc_gpu_launch_config *config);
 int icbc_gpu_get_launch_config(int level, icbc_gpu_launch_config *config);

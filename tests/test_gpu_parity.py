@@ -531,13 +531,96 @@ def test_launch_shapes_do_not_change_results(gpu_lib):
         for lv in (0, 5, 9):
             ref = ig.compress_image(img, lv, 0, (1, 1, 1), weight_mode=ig.WEIGHTS_ALPHA).cpu().numpy()
             for g, p in ig.TUNE_CANDIDATES:
-                ig.set_launch_config(lv, g, p)
-                out = ig.compress_image(img, lv, 0, (1, 1, 1), weight_mode=ig.WEIGHTS_ALPHA).cpu().numpy()
-                assert np.array_equal(out, ref), (lv, g, p)
+                for c in (ig.TUNE_CTA_WARPS if lv >= 2 else (0,)):
+                    ig.set_launch_config(lv, g, p, c)
+                    out = ig.compress_image(img, lv, 0, (1, 1, 1), weight_mode=ig.WEIGHTS_ALPHA).cpu().numpy()
+                    assert np.array_equal(out, ref), (lv, g, p, c)
         table = ig.autotune(img, levels=(1, 8), repeats=1)
         for lv in (1, 8):
-            assert (table[lv]["groups_per_warp"], table[lv]["persistent"]) == ig.get_launch_config(lv)
-            assert len(table[lv]["candidates"]) == len(ig.TUNE_CANDIDATES)
+            t = table[lv]
+            assert (t["groups_per_warp"], t["persistent"]) == ig.get_launch_config(lv)[:2]
+            assert len(t["candidates"]) == len(ig.TUNE_CANDIDATES) + (len(ig.TUNE_CTA_WARPS) if lv >= 2 else 0)
+        assert table[8]["cta_warps"] == ig.get_launch_config(8)[2] in ig.TUNE_CTA_WARPS
+        with pytest.raises(ig.IcbcGpuError):
+            ig.set_launch_config(8, 2, 0, 12)
     finally:
-        for lv, (g, p) in saved.items():
-            ig.set_launch_config(lv, g, p)
+        for lv, cfg in saved.items():
+            ig.set_launch_config(lv, *cfg)
+
+
+@pytest.mark.parametrize("cta_warps", [8, 16])
+def test_cta_wide_search_matches_oracle(gpu_lib, cta_warps):
+    """The listed pass with CTA-wide cluster searches (8 or 16 warps moving
+    through the encoder together): every block and error equals the
+    oracle's, on the hard block mixture (all block kinds, zero weights,
+    three-colour black) and the quality-sweep image, with every decoder and a
+    partial CTA group at the end of each list.  The images are large enough
+    for the CTA-wide pass (two rounds of CTAs over every SM); smaller ones
+    take 4-warp CTAs."""
+    ig = gpu_lib
+    saved = {lv: ig.get_launch_config(lv) for lv in range(10)}
+    side = 1700 if cta_warps == 16 else 1200
+    try:
+        for img, cw in ((synth.hard_mixture_image(side, side - 4, 77), (1, 1, 1)),
+                        (synth.quality_sweep_image(side - 2, side, seed=9), (0.299, 0.587, 0.114))):
+            dev = _to_dev(img)
+            for lv, decs in ((2, (0, 3)), (5, (2, 3)), (8, (1, 2)), (9, (0, 3))):
+                g, p, _ = saved[lv]
+                ig.set_launch_config(lv, g, p, cta_warps)
+                for dec in decs:
+                    out, err = ig.compress_image(dev, lv, dec, cw, weight_mode=ig.WEIGHTS_ALPHA, with_errors=True)
+                    ob, oe = O.encode_image(img, lv, dec, cw, 1, None, True, True, nthreads=os.cpu_count() or 1)
+                    assert np.array_equal(out.cpu().numpy(), ob), (lv, dec)
+                    assert same_bits(err.cpu().numpy(), oe), (lv, dec)
+    finally:
+        for lv, cfg in saved.items():
+            ig.set_launch_config(lv, *cfg)
+
+
+@pytest.mark.parametrize("cta_warps", [4, 8, 16])
+def test_batch_cta_sizes_match_oracle(gpu_lib, cta_warps):
+    """The batched form's per-level kernels at each CTA size, in one batch of
+    30 images over levels 2-9 (the per-level kernels run side by side, so a
+    CTA may serve several rounds, the last with warps that drew no task).
+    CTA rounds take consecutive tasks, which may mix images with different
+    decoders, colour weights and flags (the round then searches per warp).
+    Every image's blocks and errors equal the oracle's, on three replays."""
+    import torch
+    ig = gpu_lib
+    saved = {lv: ig.get_launch_config(lv) for lv in range(10)}
+    try:
+        for lv in range(2, 10):
+            g, p, _ = saved[lv]
+            ig.set_launch_config(lv, g, p, cta_warps)
+        rng = np.random.default_rng(23)
+        cases = []
+        for i in range(30):
+            w, h = int(rng.integers(5, 170)), int(rng.integers(5, 170))
+            img = synth.hard_mixture_image(w, h, seed=500 + i) if i % 2 else synth.quality_sweep_image(w, h, seed=i)
+            cases.append(dict(img=img, level=int(rng.integers(2, 10)), decoder=int(rng.integers(0, 4)),
+                              cw=(1.0, 1.0, 1.0) if i % 3 else (0.299, 0.587, 0.114), tcm=bool(i % 4), tcb=bool(i % 5)))
+        descs, outs, errs = [], [], []
+        for c in cases:
+            c["dev"] = _to_dev(c["img"])
+            c["oracle"] = O.encode_image(c["img"], c["level"], c["decoder"], c["cw"], 1, None, c["tcm"], c["tcb"],
+                                         nthreads=8)
+            nb = ig.blocks_of(c["img"].shape[1], c["img"].shape[0])
+            outs.append(torch.zeros((nb, 8), dtype=torch.uint8, device="cuda"))
+            errs.append(torch.zeros(nb, dtype=torch.float32, device="cuda"))
+            descs.append(ig.image_desc(c["dev"], c["level"], outs[-1], errs[-1], c["decoder"], c["cw"],
+                                       ig.WEIGHTS_ALPHA, None, c["tcm"], c["tcb"]))
+        batch = ig.Batch(descs)
+        for _ in range(3):
+            for o, e in zip(outs, errs):
+                o.zero_()
+                e.zero_()
+            batch.launch()
+            torch.cuda.synchronize()
+            for c, out, err in zip(cases, outs, errs):
+                ob, oe = c["oracle"]
+                assert np.array_equal(out.cpu().numpy(), ob), (c["level"], c["decoder"])
+                assert same_bits(err.cpu().numpy(), oe), (c["level"], c["decoder"])
+        batch.close()
+    finally:
+        for lv, cfg in saved.items():
+            ig.set_launch_config(lv, *cfg)
