@@ -512,6 +512,8 @@ def batch_leg(ig, torch, dev, args):
     def plain():
         ig.compress_images_each(plain_descs, stream)
 
+    # The batched form's CTA size, tuned on this batch (outside the timed region).
+    tuned = ig.autotune_batch(descs, stream=stream) if not args.no_autotune else None
     batch = ig.Batch(descs)
     with torch.cuda.stream(stream):
         plain()
@@ -576,7 +578,9 @@ def batch_leg(ig, torch, dev, args):
                         "per_image_psnr_min_p1_p50_p99_max": [float(psnrs.min()), q(psnrs, 1), q(psnrs, 50),
                                                               q(psnrs, 99), float(psnrs.max())],
                         "per_level": by_level},
-            "launches_plain": len(specs), "launches_batched": 1}
+            "launches_plain": len(specs), "launches_batched": 1,
+            "autotune": tuned and {"batch_cta_warps": tuned["batch_cta_warps"],
+                                   "candidates_ms": {str(k): v for k, v in tuned["candidates"].items()}}}
 
 
 def serving_leg(ig, args, batched_gpix):
@@ -597,7 +601,7 @@ def serving_leg(ig, args, batched_gpix):
         n = int(min(args.serve_max_requests, max(400, rate * args.serve_seconds)))
         reqs = synth.serving_requests(n, rate, seed=int(rate))
         outs = [np.empty((ig.blocks_of(r.side, r.side), 8), np.uint8) for r in reqs]
-        srv = ig.Server(40 << 30, max_inflight=4, max_batch_images=1024)
+        srv = ig.Server(40 << 30, max_inflight=args.serve_inflight, max_batch_images=1024)
         ids = [None] * n
         nthreads = args.serve_threads
 
@@ -632,8 +636,10 @@ def serving_leg(ig, args, batched_gpix):
                      "gpix_s": st["pixels_completed"] / wall / 1e9, "p50_ms": st["latency_p50_ms"],
                      "p99_ms": st["latency_p99_ms"], "mean_ms": st["latency_mean_ms"], "max_ms": st["latency_max_ms"],
                      "batches": st["batches"], "arena_peak_bytes": st["arena_peak"], "completed": st["completed"]})
-    return {"workload": "poisson_serving", "hbm_budget_bytes": 40 << 30, "max_inflight": 4,
-            "batched_offline_gpix_s": batched_gpix, "runs": runs}
+    return {"workload": "poisson_serving", "hbm_budget_bytes": 40 << 30, "max_inflight": args.serve_inflight,
+            "batched_offline_gpix_s": batched_gpix, "runs": runs,
+            "saturation": {"rate_req_s": runs[-1]["rate_req_s"], "gpix_s": runs[-1]["gpix_s"],
+                           "offered_gpix_s": runs[-1]["offered_gpix_s"]} if runs else None}
 
 
 def hard_leg(ig, torch, dev, args, peak_tops):
@@ -750,10 +756,12 @@ def main():
     ap.add_argument("--only-hard", action="store_true", help="run the hard-mixture leg alone (profiling)")
     ap.add_argument("--no-parity", action="store_true",
                     help="with --only-hard: skip the oracle checks and op counts (profiling)")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 5000, 20000])
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 5000, 20000, 80000],
+                    help="Poisson arrival rates; the last (80,000/s, above what the GPU encodes) measures saturation")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
-    ap.add_argument("--serve-max-requests", type=int, default=4000)
+    ap.add_argument("--serve-max-requests", type=int, default=8000)
     ap.add_argument("--serve-threads", type=int, default=4)
+    ap.add_argument("--serve-inflight", type=int, default=8, help="batched launches the server keeps on the GPU")
     args = ap.parse_args()
     if args.levels:
         global LEVELS

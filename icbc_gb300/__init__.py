@@ -55,7 +55,8 @@ class ImageDesc(ctypes.Structure):
 
 class LaunchConfig(ctypes.Structure):
     """struct icbc_gpu_launch_config."""
-    _fields_ = [("groups_per_warp", ctypes.c_int32), ("persistent", ctypes.c_int32), ("cta_warps", ctypes.c_int32)]
+    _fields_ = [("groups_per_warp", ctypes.c_int32), ("persistent", ctypes.c_int32), ("cta_warps", ctypes.c_int32),
+                ("batch_cta_warps", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -638,11 +639,58 @@ def get_launch_config(level: int) -> tuple[int, int, int]:
 
 
 def set_launch_config(level: int, groups_per_warp: int, persistent: int, cta_warps: int | None = None) -> None:
-    """Sets a level's launch shape; cta_warps None keeps the current one."""
-    if cta_warps is None:
-        cta_warps = get_launch_config(level)[2]
-    c = LaunchConfig(int(groups_per_warp), int(persistent), int(cta_warps))
+    """Sets a level's launch shape; cta_warps None keeps the current one (the
+    batched form's CTA size is kept either way)."""
+    c = LaunchConfig()
+    _check(load().icbc_gpu_get_launch_config(int(level), ctypes.byref(c)), "get_launch_config")
+    c.groups_per_warp, c.persistent = int(groups_per_warp), int(persistent)
+    if cta_warps is not None:
+        c.cta_warps = int(cta_warps)
     _check(load().icbc_gpu_set_launch_config(int(level), ctypes.byref(c)), "set_launch_config")
+
+
+def get_batch_cta_warps(level: int) -> int:
+    """The batched form's CTA size at a level (0: the default, 4)."""
+    c = LaunchConfig()
+    _check(load().icbc_gpu_get_launch_config(int(level), ctypes.byref(c)), "get_launch_config")
+    return c.batch_cta_warps
+
+
+def set_batch_cta_warps(level: int, cta_warps: int) -> None:
+    """Sets the batched form's CTA size at a level (read when a batch is created)."""
+    c = LaunchConfig()
+    _check(load().icbc_gpu_get_launch_config(int(level), ctypes.byref(c)), "get_launch_config")
+    c.batch_cta_warps = int(cta_warps)
+    _check(load().icbc_gpu_set_launch_config(int(level), ctypes.byref(c)), "set_launch_config")
+
+
+def autotune_batch(descs: Sequence[ImageDesc], candidates=TUNE_CTA_WARPS, repeats: int = 3, stream=None,
+                   apply: bool = True) -> dict:
+    """Times the batched form of `descs` (the same batch planned once per
+    candidate) with each CTA size for the per-level kernels of levels 2-9,
+    keeps the fastest (applied when `apply`) and returns {"batch_cta_warps",
+    "ms", "candidates": {cta: ms}}.  The images' outputs are overwritten."""
+    torch = _torch()
+    before = {lv: get_batch_cta_warps(lv) for lv in range(2, 10)}
+    times = {}
+    for c in candidates:
+        for lv in range(2, 10):
+            set_batch_cta_warps(lv, c)
+        b = Batch(descs)
+        b.launch(stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        e0.record(s)
+        for _ in range(repeats):
+            b.launch(stream)
+        e1.record(s)
+        torch.cuda.synchronize()
+        b.close()
+        times[c] = e0.elapsed_time(e1) / repeats
+    best = min(times, key=times.get)
+    for lv in range(2, 10):
+        set_batch_cta_warps(lv, best if apply else before[lv])
+    return {"batch_cta_warps": best, "ms": times[best], "candidates": times}
 
 
 def autotune(image, levels=range(10), candidates=TUNE_CANDIDATES, cta_candidates=TUNE_CTA_WARPS, repeats: int = 3,

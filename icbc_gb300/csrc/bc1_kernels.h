@@ -164,7 +164,8 @@ cudaError_t launch_simd(const GlobalTables *G, const ImageDesc *image, const Blo
 struct LaunchShape {
     int groups_per_warp;
     bool persistent;
-    int cta_warps;  // the listed pass's CTA size (0: the level's default)
+    int cta_warps;        // the listed pass's CTA size (0: the level's default)
+    int batch_cta_warps;  // the batched form's per-level kernel's (0: 4)
 };
 LaunchShape launch_shape(int level);
 

@@ -506,6 +506,14 @@ static int listed_cta_warps(int64_t nblocks, int sms) {
     return c > 4 && nblocks >= (int64_t)sms * 32 * c * 2 ? c : 4;
 }
 
+// The batched form's per-level kernel's CTA size: the launch shape's, else 4
+// (on a mixed batch of small images CTA-wide searches do not pay: a round's
+// tasks often differ in decoder or colour weights).
+static int batch_cta_warps() {
+    const int c = launch_shape(L).batch_cta_warps;
+    return c == 8 || c == 16 ? c : 4;
+}
+
 // Shared-memory limit of a listed-pass kernel and, once, its resident CTAs per SM.
 template <class K>
 static cudaError_t listed_attributes(K kernel, int warps, size_t smem, int *resident) {
@@ -611,7 +619,7 @@ cudaError_t ICBC_CAT(launch_batch_level_l, ICBC_LEVEL)(const GlobalTables *G, co
                                                         cudaStream_t stream, int grid, const int64_t *refine_base,
                                                         RefineSlot *slots, BatchLists lists) {
     // `grid` counts 4-warp CTAs; a CTA-wide kernel gets as many warps in all.
-    const int cta_warps = Level<L>::cluster && (L < 9 || refine_base) ? listed_cta_warps() : 4;
+    const int cta_warps = Level<L>::cluster && (L < 9 || refine_base) ? batch_cta_warps() : 4;
     if (cta_warps != 4) {
         const size_t smem = cta_warps == 16 ? batch_smem_bytes<16>() : batch_smem_bytes<8>();
         int *resident = cta_warps == 16 ? &g_resident_batch16 : &g_resident_batch8;

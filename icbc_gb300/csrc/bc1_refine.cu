@@ -43,7 +43,11 @@ __device__ __forceinline__ void load_float_block_lane(const BlocksSrc &s, int64_
 }
 
 constexpr size_t kRefineLutBytes = 256 * sizeof(float);
-constexpr size_t kRefineSmem = kRefineLutBytes + kWarpsPerCta * sizeof(float) * kWarpFloatsLow;
+// Texel rows of 68 floats (16-byte aligned, 17 float4): a texel's colour and
+// weight are one 16-byte load, and the 16-byte accesses of any 8 lanes to
+// the same texel of their rows fall in 8 different bank groups.
+constexpr int kRefineStride = 68;
+constexpr size_t kRefineSmem = kRefineLutBytes + kWarpsPerCta * sizeof(float) * 32 * kRefineStride;
 
 constexpr int kRefillBatch = 16;  // 4: 3% slower, 8: 0.4%, 12: as 16 (hard mixture, level 9)
 
@@ -76,10 +80,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
     __syncthreads();
     WarpCtx w{};
     w.D = &G->dec[p.decoder];
-    w.in = reinterpret_cast<float *>(smem + kRefineLutBytes) + (threadIdx.x >> 5) * kWarpFloatsLow;
+    w.in = reinterpret_cast<float *>(smem + kRefineLutBytes) + (threadIdx.x >> 5) * 32 * kRefineStride;
     w.lane = threadIdx.x & 31;
     const int lane = w.lane;
-    float *row = w.in + lane * kInStride;
+    float *row = w.in + lane * kRefineStride;
     EncodeParams lp = p;
     RefineLane r;
     uint2 *o = nullptr;
@@ -132,7 +136,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
                             er = errors ? errors + mine : nullptr;
                         }
                         const uint2 cur = *o;
-                        refine_begin(w, lut, FloatRow{row}, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
+                        refine_begin(w, lut, FloatRow4{row}, lp, sl.error, cur.x & 0xffff, cur.x >> 16, cur.y, r);
                         have = true;
                     }
                 }
@@ -143,7 +147,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
         bool accepted = false, stop = false;
         if (have) {
             PalF pr;
-            accepted = refine_try(w, lut, FloatRow{row}, lp, r, pr, stop);
+            accepted = refine_try(w, lut, FloatRow4{row}, lp, r, pr, stop);
             if (accepted) {
                 q0 = pr.c[0] * lp.cw;
                 q1 = pr.c[1] * lp.cw;
@@ -165,7 +169,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
             const int src = lane < 16 ? l0 : l1;
             const V3 p0 = shfl3(q0, src), p1 = shfl3(q1, src), p2 = shfl3(q2, src), p3 = shfl3(q3, src);
             const V3 cw = shfl3(lp.cw, src);
-            const uint32_t x = index_generic(FloatRow{w.in + src * kInStride}.color(lane & 15), cw, p0, p1, p2, p3);
+            const uint32_t x =
+                index_generic(FloatRow4{w.in + src * kRefineStride}.color(lane & 15), cw, p0, p1, p2, p3);
             const unsigned lo = __ballot_sync(kFull, x & 1u), hi = __ballot_sync(kFull, x >> 1);
             if (lane == l0) r.base_idx = spread_bits(lo & 0xffffu) | (spread_bits(hi & 0xffffu) << 1);
             else if (lane == l1) r.base_idx = spread_bits(lo >> 16) | (spread_bits(hi >> 16) << 1);

@@ -299,12 +299,12 @@ namespace icbc_gpu {
 int level_cost(int level) { return kLevelCost[level < 0 ? 0 : level > 9 ? 9 : level]; }
 
 // Per-level launch shapes of the plain kernels (see icbc_gpu_launch_config).
-static icbc_gpu_launch_config g_launch[10] = {{1, 1, 0}, {1, 1, 0}, {2, 0, 0}, {2, 0, 0}, {2, 0, 0},
-                                             {2, 0, 0}, {2, 0, 0}, {2, 0, 0}, {2, 0, 0}, {2, 0, 0}};
+static icbc_gpu_launch_config g_launch[10] = {{1, 1, 0, 0}, {1, 1, 0, 0}, {2, 0, 0, 0}, {2, 0, 0, 0}, {2, 0, 0, 0},
+                                             {2, 0, 0, 0}, {2, 0, 0, 0}, {2, 0, 0, 0}, {2, 0, 0, 0}, {2, 0, 0, 0}};
 
 LaunchShape launch_shape(int level) {
     const icbc_gpu_launch_config c = g_launch[level < 0 ? 0 : level > 9 ? 9 : level];
-    return LaunchShape{c.groups_per_warp, c.persistent != 0, c.cta_warps};
+    return LaunchShape{c.groups_per_warp, c.persistent != 0, c.cta_warps, c.batch_cta_warps};
 }
 }  // namespace icbc_gpu
 
@@ -376,7 +376,9 @@ int icbc_gpu_sm_count(void) { return sm_count(); }
 
 int icbc_gpu_set_launch_config(int level, const icbc_gpu_launch_config *config) {
     if (level < 0 || level > 9 || !config || config->groups_per_warp < 1 || config->groups_per_warp > 64 ||
-        !(config->cta_warps == 0 || config->cta_warps == 4 || config->cta_warps == 8 || config->cta_warps == 16))
+        !(config->cta_warps == 0 || config->cta_warps == 4 || config->cta_warps == 8 || config->cta_warps == 16) ||
+        !(config->batch_cta_warps == 0 || config->batch_cta_warps == 4 || config->batch_cta_warps == 8 ||
+          config->batch_cta_warps == 16))
         return ICBC_GPU_ERR_INVALID_ARGUMENT;
     g_launch[level] = *config;
     g_launch[level].persistent = config->persistent ? 1 : 0;

@@ -344,24 +344,27 @@ int icbc_gpu_build_mips(const uint8_t *d_rgba, int32_t width, int32_t height, in
  * level's blocks at icbc_gpu_mip_layout's offsets.  Synchronous. */
 int icbc_gpu_compress_bc1_mips(const icbc_gpu_image *image, int32_t levels, void *stream);
 
-/* Launch shape of the plain kernels of one quality level, chosen by an
- * autotuner (icbc_gb300.autotune) or set by hand.  groups_per_warp: groups
- * of 32 blocks each warp takes (1..64); persistent: 1 = exactly the
- * resident CTAs, striding over the image, 0 = enough CTAs for the work,
- * balanced by the hardware.  cta_warps (levels 2-9, RGBA8 images with
- * uniform or alpha weights, and the batched form's per-level kernels: the
- * pass that encodes the blocks of two or more colours): 4 = CTAs of 4 warps,
+/* Launch shape of the kernels of one quality level, chosen by an autotuner
+ * (icbc_gb300.autotune, icbc_gb300.autotune_batch) or set by hand.
+ * groups_per_warp: groups of 32 blocks each warp takes (1..64); persistent:
+ * 1 = exactly the resident CTAs, striding over the image, 0 = enough CTAs for
+ * the work, balanced by the hardware.  cta_warps (levels 2-9, RGBA8 images
+ * with uniform or alpha weights: the pass that encodes the blocks of two or
+ * more colours) and batch_cta_warps (the same for the batched form's kernel
+ * of that level, read when a batch is created): 4 = CTAs of 4 warps,
  * each warp searching its own 32 blocks' cluster combinations; 8 or 16 =
  * CTAs of that many warps moving through the encoder's stages together, the
  * combinations of all the CTA's blocks searched by all its threads (an image
  * too small for two rounds of such CTAs on every SM takes 4); 0 = the
  * level's default.  Defaults: 1 / persistent at levels 0-1, 2 / not
- * persistent at levels 2-9, cta_warps per level.  Not for use while launches
- * run. */
+ * persistent at levels 2-9, cta_warps 16 from level 4 on (else 4),
+ * batch_cta_warps 4.  Not for use while launches run or batches are
+ * created. */
 typedef struct icbc_gpu_launch_config {
     int32_t groups_per_warp;
     int32_t persistent;
     int32_t cta_warps;
+    int32_t batch_cta_warps;  /* 0 = 4 */
 } icbc_gpu_launch_config;
 int icbc_gpu_set_launch_config(int level, const icbc_gpu_launch_config *config);
 int icbc_gpu_get_launch_config(int level, icbc_gpu_launch_config *config);

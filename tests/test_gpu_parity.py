@@ -587,11 +587,10 @@ def test_batch_cta_sizes_match_oracle(gpu_lib, cta_warps):
     Every image's blocks and errors equal the oracle's, on three replays."""
     import torch
     ig = gpu_lib
-    saved = {lv: ig.get_launch_config(lv) for lv in range(10)}
+    saved = {lv: ig.get_batch_cta_warps(lv) for lv in range(2, 10)}
     try:
         for lv in range(2, 10):
-            g, p, _ = saved[lv]
-            ig.set_launch_config(lv, g, p, cta_warps)
+            ig.set_batch_cta_warps(lv, cta_warps)
         rng = np.random.default_rng(23)
         cases = []
         for i in range(30):
@@ -621,6 +620,10 @@ def test_batch_cta_sizes_match_oracle(gpu_lib, cta_warps):
                 assert np.array_equal(out.cpu().numpy(), ob), (c["level"], c["decoder"])
                 assert same_bits(err.cpu().numpy(), oe), (c["level"], c["decoder"])
         batch.close()
+        if cta_warps == 16:
+            table = ig.autotune_batch(descs, repeats=1)
+            assert table["batch_cta_warps"] in ig.TUNE_CTA_WARPS
+            assert all(ig.get_batch_cta_warps(lv) == table["batch_cta_warps"] for lv in range(2, 10))
     finally:
-        for lv, cfg in saved.items():
-            ig.set_launch_config(lv, *cfg)
+        for lv, c in saved.items():
+            ig.set_batch_cta_warps(lv, c)
