@@ -440,15 +440,34 @@ __device__ __forceinline__ void refine_begin(const WarpCtx &w, const float *lut,
     s.base_idx = indices_generic<4>(row, p.cw, palette_f(c0, c1, p.decoder, lut, w.D));
 }
 
+// block_error with the palette in shared memory: entry e of this lane at
+// pal[32 * e] (a warp's palettes laid out entry-major, so the 16-byte loads of
+// any 8 lanes fall in 8 bank groups whatever their indices).  One load per
+// texel instead of a 4-way select; the same floats in the same order.
+template <int UNROLL = 1, class Row>
+__device__ __forceinline__ float block_error_pal(const Row &row, V3 cw, const PalF &p, float4 *pal,
+                                                 uint32_t indices) {
+#pragma unroll
+    for (int e = 0; e < 4; e++) pal[32 * e] = make_float4(p.c[e].x, p.c[e].y, p.c[e].z, 0.0f);
+    float error = 0.0f;
+#pragma unroll UNROLL
+    for (int t = 0; t < 16; t++) {
+        const float4 q = pal[32 * ((indices >> (2 * t)) & 3)];
+        error += row.weight(t) * texel_mse(v3(q.x, q.y, q.z), row.color(t), cw);
+    }
+    return error;
+}
+
 // Iteration s.i of refine_endpoints (icbc.h:3614-3648), one trip of
 // refine()'s loop but for its index update: when the step is accepted it
 // takes the candidate and returns true with the candidate's palette in `pr`,
 // and s.base_idx must be set to indices_generic(row, cw, pr) before the next
 // iteration (the caller computes it, across lanes).  `stop`: the loop would
-// stop after this iteration.
+// stop after this iteration.  With `pal` (this lane's shared-memory palette
+// slot, block_error_pal) the step's error picks entries by a load.
 template <class Row>
 __device__ __forceinline__ bool refine_try(const WarpCtx &w, const float *lut, const Row &row, const EncodeParams &p,
-                                           RefineLane &s, PalF &pr, bool &stop) {
+                                           RefineLane &s, PalF &pr, bool &stop, float4 *pal = nullptr) {
     const int d = s.i & 15;
     const int dr = c_deltas[d][0], dg = c_deltas[d][1], db = c_deltas[d][2];
     uint32_t r0 = s.c0, r1 = s.c1;
@@ -459,7 +478,7 @@ __device__ __forceinline__ bool refine_try(const WarpCtx &w, const float *lut, c
         if (r0 < r1) { const uint32_t t = r0; r0 = r1; r1 = t; }
     }
     pr = palette_f(r0, r1, p.decoder, lut, w.D);
-    const float e = block_error<4>(row, p.cw, pr, s.base_idx);
+    const float e = pal ? block_error_pal<4>(row, p.cw, pr, pal, s.base_idx) : block_error<4>(row, p.cw, pr, s.base_idx);
     const bool accept = e < s.best;
     if (accept) {
         s.best = e;

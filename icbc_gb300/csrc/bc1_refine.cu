@@ -47,7 +47,10 @@ constexpr size_t kRefineLutBytes = 256 * sizeof(float);
 // weight are one 16-byte load, and the 16-byte accesses of any 8 lanes to
 // the same texel of their rows fall in 8 different bank groups.
 constexpr int kRefineStride = 68;
-constexpr size_t kRefineSmem = kRefineLutBytes + kWarpsPerCta * sizeof(float) * 32 * kRefineStride;
+constexpr size_t kRefineRowBytes = kWarpsPerCta * sizeof(float) * 32 * kRefineStride;
+// Then each warp's candidate palettes, 4 entries x 32 lanes of float4
+// (block_error_pal): 44 KB per CTA, five CTAs per SM.
+constexpr size_t kRefineSmem = kRefineLutBytes + kRefineRowBytes + kWarpsPerCta * 4 * 32 * sizeof(float4);
 
 constexpr int kRefillBatch = 16;  // 4: 3% slower, 8: 0.4%, 12: as 16 (hard mixture, level 9)
 
@@ -73,7 +76,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
                                                               unsigned long long *counter, const ImageDesc *images,
                                                               RefineMap map) {
     // Shared memory: the u8 table (all refinement needs of the staged
-    // tables), then each warp's 32 float texel rows -- six CTAs per SM.
+    // tables), each warp's 32 float texel rows, then its candidate palettes.
     extern __shared__ __align__(16) unsigned char smem[];
     float *lut = reinterpret_cast<float *>(smem);
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = G->s.lut255[i];
@@ -84,6 +87,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
     w.lane = threadIdx.x & 31;
     const int lane = w.lane;
     float *row = w.in + lane * kRefineStride;
+    float4 *pal = reinterpret_cast<float4 *>(smem + kRefineLutBytes + kRefineRowBytes) + (threadIdx.x >> 5) * 128 + lane;
     EncodeParams lp = p;
     RefineLane r;
     uint2 *o = nullptr;
@@ -147,7 +151,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_refine(const GlobalTables
         bool accepted = false, stop = false;
         if (have) {
             PalF pr;
-            accepted = refine_try(w, lut, FloatRow4{row}, lp, r, pr, stop);
+            accepted = refine_try(w, lut, FloatRow4{row}, lp, r, pr, stop, pal);
             if (accepted) {
                 q0 = pr.c[0] * lp.cw;
                 q1 = pr.c[1] * lp.cw;
