@@ -63,8 +63,8 @@ REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
 # flushes between kernels, as a timed call runs.  Level 8's
 # figure includes ~46 MB of write-backs of the buffer that flushes L2 before
 # the step; level 9's is its own traffic (the image is read once, through L2).
-NCU_TRAFFIC_BYTES = {8: (67.19e6 + 46.57e6) + (21.31e6 + 12.40e6),
-                     9: (16.95e6 + 9.31e6) + (22.70e6 + 7.58e6) + (13.98e6 + 8.31e6)}
+NCU_TRAFFIC_BYTES = {8: (67.18e6 + 49.04e6) + (18.72e6 + 11.34e6),
+                     9: (14.77e6 + 8.09e6) + (20.71e6 + 7.10e6) + (11.31e6 + 7.20e6)}
 TRAFFIC_SOURCE = "one ncu capture of this workload with --cache-control none: dram__bytes_read.sum + " \
                  "dram__bytes_write.sum summed over the level call's launches"
 
