@@ -169,15 +169,27 @@ def sample_rows(img: np.ndarray, stride: int) -> np.ndarray:
     return np.ascontiguousarray(np.concatenate(rows, axis=0))
 
 
-def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=None):
-    """Times the oracle (CPU restatement of the reference encoder) on the sample."""
+# The two CPU forms of the reference encoder that are timed: the scalar build
+# (ICBC_SIMD=0, the oracle's plain loops; what the reference compiles to when
+# its SIMD detection finds nothing) and the NEON build (ICBC_SIMD=-1) with its
+# cluster loops run as 4-lane vector code, as that build runs them.
+CPU_FORMS = {"scalar": {"profile": 0, "vector": False, "build": "scalar build (ICBC_SIMD=0)"},
+             "neon-vector": {"profile": 6, "vector": True,
+                             "build": "NEON build (ICBC_SIMD=-1): cluster loops as 4-lane vectors"}}
+
+
+def cpu_sweep(img_sample: np.ndarray, nthreads: int, levels=None, form: str = "scalar"):
+    """Times a CPU form of the reference encoder (the oracle, a C restatement)
+    on the sample."""
     from oracle import oracle as O
     O.lib()  # build/load outside the timed region
     levels = LEVELS if levels is None else levels
+    f = CPU_FORMS[form]
     times, stats, outs = {}, {}, {}
     for lv in levels:
         t0 = time.perf_counter()
-        b, _, st = O.encode_image(img_sample, lv, 0, CW, 1, None, True, True, nthreads=nthreads, with_stats=True)
+        b, _, st = O.encode_image(img_sample, lv, 0, CW, 1, None, True, True, nthreads=nthreads, with_stats=True,
+                                  profile=f["profile"], vector=f["vector"])
         times[lv] = time.perf_counter() - t0
         stats[lv] = st
         outs[lv] = b
@@ -270,16 +282,19 @@ def run_reference(args):
     px = sample.shape[0] * sample.shape[1]
     nthreads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_sweep(sample, nthreads, levels=[0])
+        cpu_sweep(sample, nthreads, levels=[0, 9], form=args.cpu_form)
     step_times = []
     per_level = {lv: [] for lv in LEVELS}
     for _ in range(args.steps):
-        times, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS)
+        times, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS, form=args.cpu_form)
         step_times.append(sum(times.values()))
         for lv in LEVELS:
             per_level[lv].append(times[lv])
     t = statistics.mean(step_times)
     value = len(LEVELS) * px / t / 1e9
+    # The other form, one untimed-by-the-contract sweep, for comparison.
+    other = "scalar" if args.cpu_form != "scalar" else "neon-vector"
+    otimes, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS, form=other)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
@@ -287,7 +302,9 @@ def run_reference(args):
         "config": sweep_config(args.size, ws),
         "per_level": {str(lv): len(per_level[lv]) and px / statistics.mean(per_level[lv]) / 1e9 for lv in LEVELS},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": sample_text(args.cpu_stride, px)},
+                         "sample": sample_text(args.cpu_stride, px), "build": CPU_FORMS[args.cpu_form]["build"],
+                         other: {"value": len(LEVELS) * px / sum(otimes.values()) / 1e9,
+                                 "build": CPU_FORMS[other]["build"]}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -397,7 +414,9 @@ def run_ours(args):
     sample_px = sample.shape[0] * sample.shape[1]
     nthreads = os.cpu_count() or 1
     ctimes, cstats, couts = cpu_sweep(sample, nthreads, levels=LEVELS)
-    cpu_value = len(LEVELS) * sample_px / sum(ctimes.values()) / 1e9
+    cpu_scalar = len(LEVELS) * sample_px / sum(ctimes.values()) / 1e9
+    vtimes, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS, form="neon-vector")
+    cpu_value = len(LEVELS) * sample_px / sum(vtimes.values()) / 1e9
     bw = w // 4
     rows = list(range(0, h // 4, args.cpu_stride))
     checks, quality = {}, {}
@@ -416,7 +435,8 @@ def run_ours(args):
     achieved = ops[top] / (lvl_ms[top] * 1e-3) / 1e12
     per_level = {str(lv): {"gpix_s": px / (lvl_ms[lv] * 1e-3) / 1e9, "ms": lvl_ms[lv],
                            "fp32_frac": ops[lv] / (lvl_ms[lv] * 1e-3) / 1e12 / peak,
-                           "cpu_gpix_s": sample_px / ctimes[lv] / 1e9} for lv in LEVELS}
+                           "cpu_gpix_s": sample_px / vtimes[lv] / 1e9,
+                           "cpu_scalar_gpix_s": sample_px / ctimes[lv] / 1e9} for lv in LEVELS}
     hbm = peaks.get("hbm_gbs", 6800.0)
     l0_bytes = px * 4 + nb * 8
     line = {
@@ -440,7 +460,9 @@ def run_ours(args):
                                  "unit": "GB/s", "frac": l0_bytes / (lvl_ms[0] * 1e-3) / 1e9 / hbm,
                                  "traffic": None} if 0 in lvl_ms else None),
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": sample_text(args.cpu_stride, sample_px)},
+                         "sample": sample_text(args.cpu_stride, sample_px),
+                         "build": CPU_FORMS["neon-vector"]["build"],
+                         "scalar": {"value": cpu_scalar, "build": CPU_FORMS["scalar"]["build"]}},
         "e2e": {"value": e2e["value"] if e2e else None, "unit": UNIT,
                 "h2d_bytes_per_step": e2e["h2d"] if e2e else None, "d2h_bytes_per_step": e2e["d2h"] if e2e else None,
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step",
@@ -741,6 +763,8 @@ def main():
     ap.add_argument("--levels", type=int, nargs="+", default=None,
                     help="encode only these levels (profiling); the headline uses all ten")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU leg (profiling runs)")
+    ap.add_argument("--cpu-form", default="neon-vector", choices=sorted(CPU_FORMS),
+                    help="CPU form of the reference encoder the reference arm times")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
     ap.add_argument("--batch-images", type=int, default=2000)

@@ -74,9 +74,10 @@ struct EncodeParams {
     V3 cw;
     // SIMD profile of the reference build reproduced by the profile kernels
     // (bc1_simd.cu): vector width of the cluster loops, fused vmadd/vmsub,
-    // vround01 half to even, vsaturate keeping a NaN (NEON).  The plain
+    // vround01 half to even, vsaturate keeping a NaN (NEON), and what the
+    // gather of the SAT reads past its table (fill_sat_tail).  The plain
     // kernels ignore these.
-    int simd_vec, simd_fma, simd_rne, simd_nan;
+    int simd_vec, simd_fma, simd_rne, simd_nan, simd_gather;
 };
 
 // Everything one warp needs for a group of 32 blocks.
@@ -684,10 +685,20 @@ __device__ __forceinline__ float cf3_combo_simd(const float *S, uint32_t packed,
     return dot(e1, q.metric);
 }
 
-// compute_sat's FLT_MAX fill of the entries past the colour count
-// (icbc.h:1931-1936), which the SIMD loops read for their padding lanes.
-__device__ __forceinline__ void fill_sat_tail(float *srow, int m) {
-    for (int k = m + 1; k <= 16; k++) st4(srow + 4 * k, make_float4(FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX));
+// What the SIMD loops read for their padding lanes past a SAT of m colours
+// (row entry k holds SAT slot k - 1): compute_sat's FLT_MAX fill
+// (icbc.h:1931-1936), except where the build's gather reads something else.
+// kGatherTbl: NEON's table lookups cover the first 8, 12 or 16 slots by count
+// (vqtbl2q / vqtbl3q / vqtbl4q, icbc.h:2586-2650, :2224-2270) and read zero
+// past them.  kGatherPerm8: AVX2 with m <= 8 permutes the first 8 slots
+// (permutevar8x32, icbc.h:2428-2445, :2128-2145, :867-870), index modulo 8.
+constexpr int kGatherFull = 0, kGatherTbl = 1, kGatherPerm8 = 2;
+__device__ __forceinline__ void fill_sat_tail(float *srow, int m, int gather) {
+    const int lim = gather == kGatherTbl ? (m <= 8 ? 8 : m <= 12 ? 12 : 16) : 16;
+    for (int k = m + 1; k <= 16; k++)
+        st4(srow + 4 * k, k - 1 < lim ? make_float4(FLT_MAX, FLT_MAX, FLT_MAX, FLT_MAX) : make_float4(0, 0, 0, 0));
+    if (gather == kGatherPerm8 && m <= 8)
+        for (int k = 9; k <= 16; k++) st4(srow + 4 * k, ld4(srow + 4 * (k - 8)));
 }
 
 // In a SIMD build, combination k of a block is evaluated in lane k % vec;
@@ -1057,7 +1068,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
             }
             if (O::cluster) {
                 build_sat_inplace(srow, count, false);
-                if (SIMD) fill_sat_tail(srow, count);
+                if (SIMD) fill_sat_tail(srow, count, p.simd_gather);
                 need4 = true;
             }
         }
@@ -1094,7 +1105,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
                     bool ab;
                     reduce_colors(row, O::threshold, srow, ab);
                     count3 = build_sat_inplace(srow, count, true);
-                    if (SIMD) fill_sat_tail(srow, count3);
+                    if (SIMD) fill_sat_tail(srow, count3, p.simd_gather);
                     need3 = count3 > 0;
                 } else {
                     need3 = true;

@@ -204,17 +204,21 @@ EncodeParams make_params(int decoder, int tc, int tcb, const float cw[3]) {
     p.simd_fma = 0;
     p.simd_rne = 0;
     p.simd_nan = 0;
+    p.simd_gather = kGatherFull;
     return p;
 }
 
 // Cluster-loop parameters of the reference's SIMD builds (ICBC_SIMD 0..5 and
 // -1 = NEON, icbc.h:59-66): vector width, fused vmadd/vmsub, vround01 half to
-// even, vsaturate keeping a NaN.  Index = ICBC_SIMD, NEON last.
+// even, vsaturate keeping a NaN, the SAT gather's reads past its table
+// (AVX2's permutevar8x32, NEON's table lookups).  Index = ICBC_SIMD, NEON last.
 struct SimdProfile {
-    int vec, fma, rne, nan;
+    int vec, fma, rne, nan, gather;
 };
-constexpr SimdProfile kSimdProfiles[7] = {{1, 0, 0, 0}, {4, 0, 0, 0}, {4, 0, 1, 0}, {8, 0, 1, 0},
-                                          {8, 1, 1, 0}, {16, 1, 1, 0}, {4, 0, 1, 1}};
+constexpr SimdProfile kSimdProfiles[7] = {{1, 0, 0, 0, kGatherFull},  {4, 0, 0, 0, kGatherFull},
+                                          {4, 0, 1, 0, kGatherFull},  {8, 0, 1, 0, kGatherFull},
+                                          {8, 1, 1, 0, kGatherPerm8}, {16, 1, 1, 0, kGatherFull},
+                                          {4, 0, 1, 1, kGatherTbl}};
 constexpr int kSimdNeonIndex = 6;
 
 // Table index of an ICBC_GPU_SIMD_* value, or -1 when it is not one.
@@ -228,6 +232,7 @@ static void set_simd(EncodeParams &p, int index) {
     p.simd_fma = kSimdProfiles[index].fma;
     p.simd_rne = kSimdProfiles[index].rne;
     p.simd_nan = kSimdProfiles[index].nan;
+    p.simd_gather = kSimdProfiles[index].gather;
 }
 
 // Validates an image descriptor and resolves it for the kernels.

@@ -81,9 +81,37 @@ static const float k_mid6[64] = {
  * 1..5 are ICBC_SSE2, ICBC_SSE41, ICBC_AVX1, ICBC_AVX2, ICBC_AVX512; 6 is
  * ICBC_NEON (ICBC_SIMD=-1) built without FP contraction, where vmlaq_f32 /
  * vmlsq_f32 are a multiply then an add (icbc.h:1142-1153). */
-typedef struct { int vec, fma, rne, nan; } prof_t;
-static const prof_t k_prof[7] = {{1, 0, 0, 0}, {4, 0, 0, 0}, {4, 0, 1, 0}, {8, 0, 1, 0},
-                                 {8, 1, 1, 0}, {16, 1, 1, 0}, {4, 0, 1, 1}};
+/* vx: run the cluster loops of a 4-lane profile as 4-lane vector code
+ * (cluster_fit_four_v4 / cluster_fit_three_v4), set per call from
+ * ORACLE_VECTOR_LOOPS. */
+typedef struct { int vec, fma, rne, nan, gather, vx; } prof_t;
+
+/* How a profile's cluster loops fetch SAT entry c for a lane (c >= 0).
+ * GATHER_FULL: the entry itself, FLT_MAX past the colour count (the scalar
+ * lane loads of SSE2 and AVX1, icbc.h:2652-2682; AVX-512's masked loads,
+ * icbc.h:2387-2417; SSE4.1's byte shuffles, icbc.h:2473-2522, whose
+ * out-of-table case no padding lane reaches).  GATHER_TBL: NEON's table
+ * lookups over the first 8, 12 or 16 entries by count (vqtbl2q / vqtbl3q /
+ * vqtbl4q, icbc.h:2586-2650 and :2224-2270), which read zero past the table,
+ * so the padding lanes of a 12-colour block read zero for entry 12.
+ * GATHER_PERM8: AVX2's permutevar8x32 over the first 8 entries when
+ * count <= 8 (icbc.h:2428-2445, :2128-2145, vpermuteif at :867-870), which
+ * takes the index modulo 8, so the padding lanes of an 8-colour block read
+ * entry c - 8. */
+enum { GATHER_FULL = 0, GATHER_TBL = 1, GATHER_PERM8 = 2 };
+static const prof_t k_prof[7] = {{1, 0, 0, 0, GATHER_FULL, 0},  {4, 0, 0, 0, GATHER_FULL, 0},
+                                 {4, 0, 1, 0, GATHER_FULL, 0},  {8, 0, 1, 0, GATHER_FULL, 0},
+                                 {8, 1, 1, 0, GATHER_PERM8, 0}, {16, 1, 1, 0, GATHER_FULL, 0},
+                                 {4, 0, 1, 1, GATHER_TBL, 0}};
+
+/* The SAT entry a lane of the profile reads for entry c of a count-colour
+ * SAT, -1 for a lane that reads zero. */
+static inline int p_gather(const prof_t *p, int count, int c) {
+    if (c < 0) return c;
+    if (p->gather == GATHER_TBL) return c < (count <= 8 ? 8 : count <= 12 ? 12 : 16) ? c : -1;
+    if (p->gather == GATHER_PERM8 && count <= 8) return c & 7;
+    return c;
+}
 
 static inline float p_madd(const prof_t *p, float a, float b, float c) { return p->fma ? fmaf(a, b, c) : a * b + c; }
 static inline float p_msub(const prof_t *p, float a, float b, float c) { return p->fma ? fmaf(a, b, -c) : a * b - c; }
@@ -471,7 +499,8 @@ static int lane_argmin(const float *best, int vec) {
  * minimum metric-weighted error kept.  The loop runs over whole vectors of
  * the profile's width: the combinations past the count's total come from
  * the table for larger counts (or its zero padding) and read the SAT's
- * FLT_MAX fill, as the reference's SIMD builds do. */
+ * FLT_MAX fill, or what the profile's gather reads there (p_gather), as the
+ * reference's SIMD builds do. */
 static void cluster_fit_three(const sat_t *sat, int count, v3 metric_sqr, const prof_t *pf, v3 *start, v3 *end,
                               oracle_stats *st) {
     const float r_sum = sat->r[count - 1], g_sum = sat->g[count - 1], b_sum = sat->b[count - 1], w_sum = sat->w[count - 1];
@@ -484,7 +513,8 @@ static void cluster_fit_three(const sat_t *sat, int count, v3 metric_sqr, const 
         const int l = i % pf->vec;
         v3 x0 = {0, 0, 0}, x1 = {0, 0, 0};
         float w0 = 0, w1 = 0;
-        int c0 = (i < 152 ? g_three[i][0] : 0) - 1, c1 = (i < 152 ? g_three[i][1] : 0) - 1;
+        int c0 = p_gather(pf, count, (i < 152 ? g_three[i][0] : 0) - 1);
+        int c1 = p_gather(pf, count, (i < 152 ? g_three[i][1] : 0) - 1);
         if (c0 >= 0) { x0 = v3_make(sat->r[c0], sat->g[c0], sat->b[c0]); w0 = sat->w[c0]; }
         if (c1 >= 0) { x1 = v3_make(sat->r[c1], sat->g[c1], sat->b[c1]); w1 = sat->w[c1]; }
         float w2 = w_sum - w1;
@@ -537,8 +567,9 @@ static void cluster_fit_four(const sat_t *sat, int count, v3 metric_sqr, const d
         const int l = i % pf->vec;
         v3 x0 = {0, 0, 0}, x1 = {0, 0, 0}, x2 = {0, 0, 0};
         float w0 = 0, w1 = 0, w2 = 0;
-        int c0 = (i < 968 ? g_four[i][0] : 0) - 1, c1 = (i < 968 ? g_four[i][1] : 0) - 1;
-        int c2 = (i < 968 ? g_four[i][2] : 0) - 1;
+        int c0 = p_gather(pf, count, (i < 968 ? g_four[i][0] : 0) - 1);
+        int c1 = p_gather(pf, count, (i < 968 ? g_four[i][1] : 0) - 1);
+        int c2 = p_gather(pf, count, (i < 968 ? g_four[i][2] : 0) - 1);
         if (c0 >= 0) { x0 = v3_make(sat->r[c0], sat->g[c0], sat->b[c0]); w0 = sat->w[c0]; }
         if (c1 >= 0) { x1 = v3_make(sat->r[c1], sat->g[c1], sat->b[c1]); w1 = sat->w[c1]; }
         if (c2 >= 0) { x2 = v3_make(sat->r[c2], sat->g[c2], sat->b[c2]); w2 = sat->w[c2]; }
@@ -579,6 +610,191 @@ static void cluster_fit_four(const sat_t *sat, int count, v3 metric_sqr, const d
     const int w = lane_argmin(best, pf->vec);
     *start = bs[w];
     *end = be[w];
+}
+
+/* ------------------------------------------- cluster fit, 4-lane vectors */
+
+/* cluster_fit_four / cluster_fit_three of a 4-lane profile (SSE2, SSE4.1,
+ * NEON) run four combinations at a time in GCC vector types, the way the
+ * reference's 4-lane builds run them (VFloat, icbc.h:427-668 for SSE,
+ * :1121-1235 for NEON): combination i in lane i % 4, each lane keeping its
+ * first strict minimum, then lane_argmin.  Every lane operation is the IEEE
+ * operation of the scalar-lane loops above, in the same order and without
+ * contraction (this file is built with -ffp-contract=off), and the SAT
+ * entries come through the same p_gather, so both loops give the same bits;
+ * these exist to time a vectorised CPU encoder.  The vector types compile to
+ * NEON on aarch64 and to SSE2 on x86-64, with no target intrinsics. */
+typedef float f4 __attribute__((vector_size(16)));
+typedef int32_t i4 __attribute__((vector_size(16)));
+
+static inline f4 f4_1(float x) { f4 r = {x, x, x, x}; return r; }
+static inline f4 f4_sel(i4 m, f4 a, f4 b) { return (f4)(((i4)a & m) | ((i4)b & ~m)); }
+
+/* p_saturate: tmin(tmax(a, 0), 1) with the template's comparisons (a NaN
+ * goes to 0), the NaN kept on NEON. */
+static inline f4 f4_saturate(const prof_t *p, f4 a) {
+    const f4 z = f4_1(0.0f), o = f4_1(1.0f);
+    f4 x = f4_sel(z < a, a, z);
+    x = f4_sel(x < o, x, o);
+    return p->nan ? f4_sel(a != a, a, x) : x;
+}
+
+/* p_round01 of 0 <= a <= 63 (or a NaN): half to even through the 2^23
+ * addition, exact in that range, or int(a + 0.5f). */
+static inline f4 f4_round01(const prof_t *p, f4 a) {
+    if (p->rne) return (a + f4_1(8388608.0f)) - f4_1(8388608.0f);
+    return __builtin_convertvector(__builtin_convertvector(a + f4_1(0.5f), i4), f4);
+}
+
+static inline void f4_round_ept(const prof_t *p, f4 *x, f4 *y, f4 *z) {
+    *x = f4_round01(p, f4_saturate(p, *x) * f4_1(31.0f)) * f4_1(1.0f / 31.0f);
+    *y = f4_round01(p, f4_saturate(p, *y) * f4_1(63.0f)) * f4_1(1.0f / 63.0f);
+    *z = f4_round01(p, f4_saturate(p, *z) * f4_1(31.0f)) * f4_1(1.0f / 31.0f);
+}
+
+/* The SAT as 17 (r, g, b, w) vectors indexed by a cluster table entry:
+ * entry 0 reads zero, entry e the SAT slot e - 1 as the profile gathers it. */
+static void f4_sat_table(const prof_t *p, const sat_t *sat, int count, f4 tt[17]) {
+    tt[0] = f4_1(0.0f);
+    for (int e = 1; e <= 16; e++) {
+        const int c = p_gather(p, count, e - 1);
+        if (c < 0) {
+            tt[e] = f4_1(0.0f);
+        } else {
+            f4 v = {sat->r[c], sat->g[c], sat->b[c], sat->w[c]};
+            tt[e] = v;
+        }
+    }
+}
+
+/* Four lanes' SAT entries e[0], e[stride], e[2 stride], e[3 stride] as
+ * channel vectors (a 4x4 transpose). */
+static inline void f4_gather(const f4 *tt, const uint8_t *e, int stride, f4 *r, f4 *g, f4 *b, f4 *w) {
+    const f4 A = tt[e[0]], B = tt[e[stride]], C = tt[e[2 * stride]], D = tt[e[3 * stride]];
+    const i4 lo = {0, 4, 1, 5}, hi = {2, 6, 3, 7}, l2 = {0, 1, 4, 5}, h2 = {2, 3, 6, 7};
+    const f4 t0 = __builtin_shuffle(A, B, lo), t1 = __builtin_shuffle(A, B, hi);
+    const f4 t2 = __builtin_shuffle(C, D, lo), t3 = __builtin_shuffle(C, D, hi);
+    *r = __builtin_shuffle(t0, t2, l2);
+    *g = __builtin_shuffle(t0, t2, h2);
+    *b = __builtin_shuffle(t1, t3, l2);
+    *w = __builtin_shuffle(t1, t3, h2);
+}
+
+/* The least-squares endpoints, their 565 snap and the metric-weighted error
+ * of four combinations (the common tail of icbc.h:2299-2323 and
+ * :2697-2733); keeps each lane's first strict minimum. */
+typedef struct { f4 best, ar, ag, ab, br, bg, bb; } f4_keep;
+
+static inline void f4_fit(const prof_t *p, f4 alpha2, f4 beta2, f4 alphabeta, f4 axr, f4 axg, f4 axb, f4 bxr,
+                          f4 bxg, f4 bxb, f4 mr, f4 mg, f4 mb, f4_keep *k) {
+    const f4 factor = f4_1(1.0f) / (alpha2 * beta2 - alphabeta * alphabeta);
+    f4 ar = (axr * beta2 - bxr * alphabeta) * factor;
+    f4 ag = (axg * beta2 - bxg * alphabeta) * factor;
+    f4 ab = (axb * beta2 - bxb * alphabeta) * factor;
+    f4 br = (bxr * alpha2 - axr * alphabeta) * factor;
+    f4 bg = (bxg * alpha2 - axg * alphabeta) * factor;
+    f4 bb = (bxb * alpha2 - axb * alphabeta) * factor;
+    f4_round_ept(p, &ar, &ag, &ab);
+    f4_round_ept(p, &br, &bg, &bb);
+    const f4 two = f4_1(2.0f);
+    const f4 e2r = (ar * (br * alphabeta - axr) - br * bxr) * two;
+    const f4 e2g = (ag * (bg * alphabeta - axg) - bg * bxg) * two;
+    const f4 e2b = (ab * (bb * alphabeta - axb) - bb * bxb) * two;
+    const f4 e1r = (ar * ar) * alpha2 + ((br * br) * beta2 + e2r);
+    const f4 e1g = (ag * ag) * alpha2 + ((bg * bg) * beta2 + e2g);
+    const f4 e1b = (ab * ab) * alpha2 + ((bb * bb) * beta2 + e2b);
+    const f4 error = e1r * mr + e1g * mg + e1b * mb;
+    const i4 m = error < k->best;
+    k->best = f4_sel(m, error, k->best);
+    k->ar = f4_sel(m, ar, k->ar);
+    k->ag = f4_sel(m, ag, k->ag);
+    k->ab = f4_sel(m, ab, k->ab);
+    k->br = f4_sel(m, br, k->br);
+    k->bg = f4_sel(m, bg, k->bg);
+    k->bb = f4_sel(m, bb, k->bb);
+}
+
+static void f4_keep_init(f4_keep *k) {
+    k->best = f4_1(FLT_MAX);
+    k->ar = k->ag = k->ab = k->br = k->bg = k->bb = f4_1(0.0f);
+}
+
+static void f4_keep_result(const f4_keep *k, v3 *start, v3 *end) {
+    float best[4];
+    for (int l = 0; l < 4; l++) best[l] = k->best[l];
+    const int w = lane_argmin(best, 4);
+    *start = v3_make(k->ar[w], k->ag[w], k->ab[w]);
+    *end = v3_make(k->br[w], k->bg[w], k->bb[w]);
+}
+
+static void cluster_fit_three_v4(const sat_t *sat, int count, v3 metric_sqr, const prof_t *pf, v3 *start, v3 *end,
+                                 oracle_stats *st) {
+    f4 tt[17];
+    f4_sat_table(pf, sat, count, tt);
+    const f4 r_sum = f4_1(sat->r[count - 1]), g_sum = f4_1(sat->g[count - 1]), b_sum = f4_1(sat->b[count - 1]);
+    const f4 w_sum = f4_1(sat->w[count - 1]);
+    const f4 mr = f4_1(metric_sqr.x), mg = f4_1(metric_sqr.y), mb = f4_1(metric_sqr.z);
+    const f4 quarter = f4_1(0.25f), half = f4_1(0.5f);
+    f4_keep k;
+    f4_keep_init(&k);
+    const int total = g_three_total[count - 1];
+    const int padded = (total + 3) & ~3;
+    for (int i = 0; i < padded; i += 4) {
+        f4 x0r, x0g, x0b, w0, x1r, x1g, x1b, w1;
+        f4_gather(tt, &g_three[i][0], 2, &x0r, &x0g, &x0b, &w0);
+        f4_gather(tt, &g_three[i][1], 2, &x1r, &x1g, &x1b, &w1);
+        const f4 w2 = w_sum - w1;
+        x1r = x1r - x0r;
+        x1g = x1g - x0g;
+        x1b = x1b - x0b;
+        w1 = w1 - w0;
+        const f4 alphabeta = w1 * quarter;
+        const f4 alpha2 = w0 + alphabeta;
+        const f4 beta2 = w2 + alphabeta;
+        const f4 axr = x0r + x1r * half, axg = x0g + x1g * half, axb = x0b + x1b * half;
+        f4_fit(pf, alpha2, beta2, alphabeta, axr, axg, axb, r_sum - axr, g_sum - axg, b_sum - axb, mr, mg, mb, &k);
+    }
+    if (st) st->cf3_combos += total;
+    f4_keep_result(&k, start, end);
+}
+
+static void cluster_fit_four_v4(const sat_t *sat, int count, v3 metric_sqr, const dec_tables *dt, const prof_t *pf,
+                                v3 *start, v3 *end, oracle_stats *st) {
+    f4 tt[17];
+    f4_sat_table(pf, sat, count, tt);
+    const f4 r_sum = f4_1(sat->r[count - 1]), g_sum = f4_1(sat->g[count - 1]), b_sum = f4_1(sat->b[count - 1]);
+    const f4 w_sum = f4_1(sat->w[count - 1]);
+    const f4 w1_3 = f4_1(dt->w1_3), w2_3 = f4_1(dt->w2_3), w1_9 = f4_1(dt->w1_9), w4_9 = f4_1(dt->w4_9);
+    const f4 w2_9 = f4_1(dt->w2_9);
+    const f4 mr = f4_1(metric_sqr.x), mg = f4_1(metric_sqr.y), mb = f4_1(metric_sqr.z);
+    f4_keep k;
+    f4_keep_init(&k);
+    const int total = g_four_total[count - 1];
+    const int padded = (total + 3) & ~3;
+    for (int i = 0; i < padded; i += 4) {
+        f4 x0r, x0g, x0b, w0, x1r, x1g, x1b, w1, x2r, x2g, x2b, w2;
+        f4_gather(tt, &g_four[i][0], 3, &x0r, &x0g, &x0b, &w0);
+        f4_gather(tt, &g_four[i][1], 3, &x1r, &x1g, &x1b, &w1);
+        f4_gather(tt, &g_four[i][2], 3, &x2r, &x2g, &x2b, &w2);
+        const f4 w3 = w_sum - w2;
+        x2r = x2r - x1r;
+        x2g = x2g - x1g;
+        x2b = x2b - x1b;
+        x1r = x1r - x0r;
+        x1g = x1g - x0g;
+        x1b = x1b - x0b;
+        w2 = w2 - w1;
+        w1 = w1 - w0;
+        const f4 alpha2 = w2 * w1_9 + (w1 * w4_9 + w0);
+        const f4 beta2 = w1 * w1_9 + (w2 * w4_9 + w3);
+        const f4 alphabeta = (w1 + w2) * w2_9;
+        const f4 axr = x2r * w1_3 + (x1r * w2_3 + x0r);
+        const f4 axg = x2g * w1_3 + (x1g * w2_3 + x0g);
+        const f4 axb = x2b * w1_3 + (x1b * w2_3 + x0b);
+        f4_fit(pf, alpha2, beta2, alphabeta, axr, axg, axb, r_sum - axr, g_sum - axg, b_sum - axb, mr, mg, mb, &k);
+    }
+    if (st) st->cf4_combos += total;
+    f4_keep_result(&k, start, end);
 }
 
 /* ------------------------------------------------------ error evaluation */
@@ -779,7 +995,10 @@ static float cluster_fit(const float *in, const float *in_w, const v3 *colors, c
     sat_t sat;
     int sat_count = compute_sat(colors, weights, count, &sat, st);
     v3 start, end;
-    cluster_fit_four(&sat, sat_count, metric_sqr, dt, pf, &start, &end, st);
+    if (pf->vx)
+        cluster_fit_four_v4(&sat, sat_count, metric_sqr, dt, pf, &start, &end, st);
+    else
+        cluster_fit_four(&sat, sat_count, metric_sqr, dt, pf, &start, &end, st);
     float best = output_block4(in, in_w, cw, start, end, decoder, out, st);
     if (three_color_mode) {
         if (try_black) {
@@ -789,7 +1008,10 @@ static float cluster_fit(const float *in, const float *in_w, const v3 *colors, c
             if (!tcount) return best;
             sat_count = compute_sat(tc, tw, tcount, &sat, st);
         }
-        cluster_fit_three(&sat, sat_count, metric_sqr, pf, &start, &end, st);
+        if (pf->vx)
+            cluster_fit_three_v4(&sat, sat_count, metric_sqr, pf, &start, &end, st);
+        else
+            cluster_fit_three(&sat, sat_count, metric_sqr, pf, &start, &end, st);
         blk b3;
         float e3 = output_block3(in, in_w, cw, allow_black, start, end, decoder, &b3, st);
         if (e3 < best) { best = e3; *out = b3; }
@@ -889,7 +1111,9 @@ float oracle_compress_bc1(int decoder, int level, const float *in, const float *
                           int three_color_mode, int three_color_black, void *outp, oracle_stats *st) {
     oracle_init();
     int profile = (decoder >> ORACLE_PROFILE_SHIFT) & 7;
-    const prof_t *pf = &k_prof[profile < 7 ? profile : 0];
+    prof_t prof = k_prof[profile < 7 ? profile : 0];
+    prof.vx = (decoder & ORACLE_VECTOR_LOOPS) && prof.vec == 4;
+    const prof_t *pf = &prof;
     decoder &= 3;
     const dec_tables *dt = &g_dec[decoder];
     options opt = setup_options(level, three_color_mode, three_color_black);

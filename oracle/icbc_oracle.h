@@ -34,6 +34,10 @@ enum { ORACLE_D3D10 = 0, ORACLE_NVIDIA = 1, ORACLE_AMD = 2, ORACLE_INTEL = 3 };
  * by vsaturate), each compiled without FP contraction.  Nothing else in the
  * encoder depends on ICBC_SIMD. */
 #define ORACLE_PROFILE_SHIFT 8
+/* With a 4-lane profile (SSE2, SSE4.1, NEON), this bit of `decoder` runs the
+ * cluster loops as 4-lane vector code: the same results, a vectorised CPU
+ * encoder to time.  Ignored with the other profiles. */
+#define ORACLE_VECTOR_LOOPS (1 << 11)
 enum { ORACLE_SCALAR = 0, ORACLE_SSE2 = 1, ORACLE_SSE41 = 2, ORACLE_AVX1 = 3, ORACLE_AVX2 = 4, ORACLE_AVX512 = 5,
        ORACLE_NEON = 6 };
 

@@ -33,6 +33,13 @@ _ref = {}
 
 PROFILE_SHIFT = 8
 PROFILES = {"scalar": 0, "sse2": 1, "sse41": 2, "avx": 3, "avx2": 4, "avx512": 5, "neon": 6}
+# ORACLE_VECTOR_LOOPS: the cluster loops of a 4-lane profile as 4-lane vector
+# code (same results; a vectorised CPU encoder to time).
+VECTOR_LOOPS = 1 << 11
+
+
+def _decoder_word(decoder, profile, vector):
+    return int(decoder) | (int(profile) << PROFILE_SHIFT) | (VECTOR_LOOPS if vector else 0)
 
 
 def ref_path(profile: int = 0) -> str:
@@ -180,9 +187,10 @@ def _cw(color_weights):
 
 
 def compress_blocks(colors, weights, level, decoder=0, color_weights=(1, 1, 1), three_color_mode=True,
-                    three_color_black=True, nthreads=1, out=None, with_stats=False, profile=0):
+                    three_color_black=True, nthreads=1, out=None, with_stats=False, profile=0, vector=False):
     """Oracle encode of n blocks.  colors: (n,16,4) float32; weights: (n,16) or None.
-    Returns (blocks uint8 (n,8), errors float32 (n,)[, stats dict])."""
+    Returns (blocks uint8 (n,8), errors float32 (n,)[, stats dict]).  vector:
+    run a 4-lane profile's cluster loops as vector code."""
     L = lib()
     colors = _f32(colors).reshape(-1, 64)
     n = colors.shape[0]
@@ -191,7 +199,7 @@ def compress_blocks(colors, weights, level, decoder=0, color_weights=(1, 1, 1), 
     err = np.zeros(n, np.float32)
     cw, cwp = _cw(color_weights)
     st = Stats()
-    L.oracle_compress_blocks(int(decoder) | (int(profile) << PROFILE_SHIFT), int(level), colors.ctypes.data,
+    L.oracle_compress_blocks(_decoder_word(decoder, profile, vector), int(level), colors.ctypes.data,
                              None if w is None else w.ctypes.data,
                              cwp, int(bool(three_color_mode)), int(bool(three_color_black)), out.ctypes.data,
                              err.ctypes.data, n, int(nthreads), ctypes.byref(st))
@@ -199,8 +207,10 @@ def compress_blocks(colors, weights, level, decoder=0, color_weights=(1, 1, 1), 
 
 
 def encode_image(rgba, level, decoder=0, color_weights=(1, 1, 1), weight_mode=0, weight_plane=None,
-                 three_color_mode=True, three_color_black=True, nthreads=1, with_stats=False, profile=0):
-    """Oracle encode of an RGBA8 image (h, w, 4) uint8 -> (blocks (nb,8), errors (nb,))."""
+                 three_color_mode=True, three_color_black=True, nthreads=1, with_stats=False, profile=0,
+                 vector=False):
+    """Oracle encode of an RGBA8 image (h, w, 4) uint8 -> (blocks (nb,8), errors (nb,)).
+    vector: run a 4-lane profile's cluster loops as vector code."""
     L = lib()
     rgba = np.ascontiguousarray(rgba, dtype=np.uint8)
     h, w = rgba.shape[:2]
@@ -211,7 +221,7 @@ def encode_image(rgba, level, decoder=0, color_weights=(1, 1, 1), weight_mode=0,
     plane = None if weight_plane is None else _f32(weight_plane).reshape(h, w)
     st = Stats()
     L.oracle_encode_image(rgba.ctypes.data, w, h, w * 4, int(weight_mode),
-                          None if plane is None else plane.ctypes.data, int(decoder) | (int(profile) << PROFILE_SHIFT),
+                          None if plane is None else plane.ctypes.data, _decoder_word(decoder, profile, vector),
                           int(level), cwp,
                           int(bool(three_color_mode)), int(bool(three_color_black)), out.ctypes.data,
                           err.ctypes.data, int(nthreads), ctypes.byref(st))

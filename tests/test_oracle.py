@@ -150,6 +150,56 @@ def test_oracle_neon_profile():
     assert 0 < (a != b).any(1).sum() < 4000
 
 
+def _exact_colour_blocks(n, ncol, seed):
+    """n blocks of exactly ncol distinct colours (half of them close
+    together), with weights mixing 1 and random values."""
+    rng = np.random.default_rng(seed)
+    pal = rng.integers(0, 256, (n, ncol, 3))
+    pal[: n // 2] = np.clip(pal[: n // 2, :1] + rng.integers(-20, 21, (n // 2, ncol, 3)), 0, 255)
+    idx = np.concatenate([np.tile(np.arange(ncol), (n, 1)), rng.integers(0, ncol, (n, 16 - ncol))], 1)
+    idx = rng.permuted(idx, axis=1)
+    cols = np.ones((n, 16, 4), np.float32)
+    cols[:, :, :3] = np.take_along_axis(pal, idx[:, :, None], 1) / 255.0
+    w = np.where(rng.random((n, 16)) < 0.5, 1.0, rng.random((n, 16))).astype(np.float32)
+    return cols, w
+
+
+@pytest.mark.parametrize("profile", ["sse2", "sse41", "neon"])
+def test_oracle_vector_loops_match_lane_loops(profile):
+    """The 4-lane vector form of the cluster loops (the timed CPU encoder)
+    against the scalar-lane form, bit for bit: mixed blocks, blocks of exactly
+    8 and 12 colours (where AVX2's and NEON's gathers read past their tables),
+    extreme weights (NaN combinations, kept by NEON's vsaturate)."""
+    pr = O.PROFILES[profile]
+    sets = [synth.mixed_blocks(600, seed=31), _exact_colour_blocks(400, 8, 32), _exact_colour_blocks(400, 12, 33),
+            synth.extreme_weight_blocks(600, seed=34)]
+    for cols, w in sets:
+        for lvl in (1, 5, 7, 9):
+            for dec in (0, 1):
+                for tc, tcb in SIMD_FLAGS:
+                    a, ea = O.compress_blocks(cols, w, lvl, dec, (1, .7, .3), tc, tcb, nthreads=4, profile=pr)
+                    b, eb = O.compress_blocks(cols, w, lvl, dec, (1, .7, .3), tc, tcb, nthreads=4, profile=pr,
+                                              vector=True)
+                    assert np.array_equal(a, b), (profile, lvl, dec, tc, tcb)
+                    assert np.array_equal(ea.view(np.uint32), eb.view(np.uint32)), (profile, lvl, dec, tc, tcb)
+
+
+@pytest.mark.parametrize("profile", [1, 2])
+def test_oracle_vector_loops_match_golden(profile):
+    """The vector form under the SSE2 and SSE4.1 profiles against the golden
+    vectors of the reference's own SSE2 and SSE4.1 builds."""
+    g = np.load(os.path.join(GOLDEN, "simd.npz"))
+    for si in range(2):
+        cols, wt, cw = g["set%d_colors" % si], g["set%d_weights" % si], tuple(g["set%d_cw" % si])
+        for lvl in SIMD_LEVELS:
+            for dec in range(4):
+                for tc, tcb in SIMD_FLAGS:
+                    key = "set%d_P%d_L%d_D%d_tc%d_tcb%d" % (si, profile, lvl, dec, tc, tcb)
+                    b, e = O.compress_blocks(cols, wt, lvl, dec, cw, tc, tcb, profile=profile, vector=True)
+                    assert np.array_equal(b, g[key + "_blocks"]), key
+                    assert np.array_equal(e.view(np.uint32), g[key + "_errors"].view(np.uint32)), key
+
+
 @pytest.mark.parametrize("profile", range(1, 6))
 def test_oracle_simd_profiles_match_compiled_builds(profile):
     """The same against the SIMD builds themselves on other blocks (x86 hosts
