@@ -528,7 +528,32 @@ __device__ __forceinline__ FitWeights fit_weights(const DecoderTables *D, V3 met
     return k;
 }
 
+// The metric-weighted error of a combination's snapped endpoints
+// (icbc.h:2317-2323, :2715-2722): e2 = (a * (b * ab - ax) - b * bx) * 2,
+// e1 = (a * a) * alpha2 + ((b * b) * beta2 + e2), dot(e1, metric).  BND:
+// the product by 2 folds into the sum as one fused multiply-add (exact).
+template <bool BND>
+__device__ __forceinline__ float fit_error(V3 a, V3 b, V3 ax, V3 bx, float alpha2, float beta2, float ab, V3 metric) {
+    const V3 t = v3(a.x * (b.x * ab - ax.x) - b.x * bx.x, a.y * (b.y * ab - ax.y) - b.y * bx.y,
+                    a.z * (b.z * ab - ax.z) - b.z * bx.z);
+    V3 e1;
+    if (BND) {
+        e1 = v3((a.x * a.x) * alpha2 + __fmaf_rn(t.x, 2.0f, (b.x * b.x) * beta2),
+                (a.y * a.y) * alpha2 + __fmaf_rn(t.y, 2.0f, (b.y * b.y) * beta2),
+                (a.z * a.z) * alpha2 + __fmaf_rn(t.z, 2.0f, (b.z * b.z) * beta2));
+    } else {
+        e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + t.x * 2.0f),
+                (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + t.y * 2.0f),
+                (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + t.z * 2.0f));
+    }
+    return dot(e1, metric);
+}
+
 // One cluster_fit_four iteration (icbc.h:2650-2722), scalar arithmetic order.
+// BND (inputs of a kBounded row): e2 = t * 2 enters e1 only through
+// (b * b) * beta2 + e2, and t * 2 is exact when t cannot overflow, so the
+// product and that sum are one fused multiply-add with the same bits.
+template <bool BND = false>
 __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                           V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff, i2 = packed >> 16;
@@ -552,15 +577,13 @@ __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, cons
                      (ax.z * beta2 - bx.z * ab) * factor));
     b = round_ept(v3((bx.x * alpha2 - ax.x * ab) * factor, (bx.y * alpha2 - ax.y * ab) * factor,
                      (bx.z * alpha2 - ax.z * ab) * factor));
-    const V3 e2 = v3((a.x * (b.x * ab - ax.x) - b.x * bx.x) * 2.0f, (a.y * (b.y * ab - ax.y) - b.y * bx.y) * 2.0f,
-                     (a.z * (b.z * ab - ax.z) - b.z * bx.z) * 2.0f);
-    const V3 e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + e2.x),
-                     (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + e2.y),
-                     (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + e2.z));
-    return dot(e1, q.metric);
+    return fit_error<BND>(a, b, ax, bx, alpha2, beta2, ab, q.metric);
 }
 
-// One cluster_fit_three iteration (icbc.h:2273-2323).
+// One cluster_fit_three iteration (icbc.h:2273-2323).  BND: as cf4_combo,
+// and x1 * 0.5 is exact (never denormal), so alphax_sum = x0 + x1 * 0.5 is
+// one fused multiply-add.
+template <bool BND = false>
 __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                           V3 &a, V3 &b) {
     const int i0 = packed & 0xff, i1 = (packed >> 8) & 0xff;
@@ -576,18 +599,14 @@ __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, cons
     const float alpha2 = w0 + ab;
     const float beta2 = w2 + ab;
     const float factor = 1.0f / (alpha2 * beta2 - ab * ab);
-    const V3 ax = x0 + x1 * 0.5f;
+    const V3 ax = BND ? v3(__fmaf_rn(x1.x, 0.5f, x0.x), __fmaf_rn(x1.y, 0.5f, x0.y), __fmaf_rn(x1.z, 0.5f, x0.z))
+                      : x0 + x1 * 0.5f;
     const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
     a = round_ept(v3((ax.x * beta2 - bx.x * ab) * factor, (ax.y * beta2 - bx.y * ab) * factor,
                      (ax.z * beta2 - bx.z * ab) * factor));
     b = round_ept(v3((bx.x * alpha2 - ax.x * ab) * factor, (bx.y * alpha2 - ax.y * ab) * factor,
                      (bx.z * alpha2 - ax.z * ab) * factor));
-    const V3 e2 = v3((a.x * (b.x * ab - ax.x) - b.x * bx.x) * 2.0f, (a.y * (b.y * ab - ax.y) - b.y * bx.y) * 2.0f,
-                     (a.z * (b.z * ab - ax.z) - b.z * bx.z) * 2.0f);
-    const V3 e1 = v3((a.x * a.x) * alpha2 + ((b.x * b.x) * beta2 + e2.x),
-                     (a.y * a.y) * alpha2 + ((b.y * b.y) * beta2 + e2.y),
-                     (a.z * a.z) * alpha2 + ((b.z * b.z) * beta2 + e2.z));
-    return dot(e1, q.metric);
+    return fit_error<BND>(a, b, ax, bx, alpha2, beta2, ab, q.metric);
 }
 
 // ----------------------------------------------- SIMD-profile cluster fit --
@@ -835,7 +854,7 @@ __device__ __forceinline__ void walker_cross(const WarpCtx &w, Walker &v, uint32
 
 // Returns this lane's winning table index, or -1 (no search, or no error
 // below FLT_MAX: the reference then keeps zero endpoints).
-template <bool FOUR, bool SIMD = false>
+template <bool FOUR, bool SIMD = false, bool BND = false>
 __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int count, const FitWeights &q,
                                            const EncodeParams *p = nullptr) {
     const int lane = w.lane;
@@ -875,8 +894,8 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
             eb = FOUR ? cf4_combo_simd(B.S, pb, B.sums, q, f, rne, nan, a, b)
                       : cf3_combo_simd(B.S, pb, B.sums, q, f, rne, nan, a, b);
         } else {
-            ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
-            eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
+            ea = FOUR ? cf4_combo<BND>(A.S, pa, A.sums, q, a, b) : cf3_combo<BND>(A.S, pa, A.sums, q, a, b);
+            eb = FOUR ? cf4_combo<BND>(B.S, pb, B.sums, q, a, b) : cf3_combo<BND>(B.S, pb, B.sums, q, a, b);
         }
         walker_fold<SIMD>(A, ea, vec);
         walker_fold<SIMD>(B, eb, vec);
@@ -904,7 +923,7 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 // the CTA must call it together (it synchronises the CTA) with the same fit
 // weights `q`: every thread walks combinations of any of the group's blocks.
 // Same winner rule as flat_search: per block the smallest (error, table index).
-template <bool FOUR, int NW>
+template <bool FOUR, int NW, bool BND = false>
 __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bool need, int count,
                                                  const FitWeights &q) {
     const int j = threadIdx.x;
@@ -938,8 +957,8 @@ __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bo
     for (int it = 0; it < per; it++) {
         uint32_t na = table[A.k + 1], nb = table[B.k + 1];
         V3 a, b;
-        const float ea = FOUR ? cf4_combo(A.S, pa, A.sums, q, a, b) : cf3_combo(A.S, pa, A.sums, q, a, b);
-        const float eb = FOUR ? cf4_combo(B.S, pb, B.sums, q, a, b) : cf3_combo(B.S, pb, B.sums, q, a, b);
+        const float ea = FOUR ? cf4_combo<BND>(A.S, pa, A.sums, q, a, b) : cf3_combo<BND>(A.S, pa, A.sums, q, a, b);
+        const float eb = FOUR ? cf4_combo<BND>(B.S, pb, B.sums, q, a, b) : cf3_combo<BND>(B.S, pb, B.sums, q, a, b);
         walker_fold(A, ea);
         walker_fold(B, eb);
         const bool xa = walker_crossing(A), xb = walker_crossing(B);
@@ -1080,8 +1099,8 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         // 4-colour cluster fit of every block that needs one, across the warp.
         const FitWeights q = fit_weights(w.D, metric);
         int my4;
-        if (NW > 1 && group) my4 = flat_search_group<true, NW>(*g, gsums, need4, count, q);
-        else my4 = flat_search<true, SIMD>(w, need4, count, q, &p);
+        if (NW > 1 && group) my4 = flat_search_group<true, NW, Row::kBounded>(*g, gsums, need4, count, q);
+        else my4 = flat_search<true, SIMD, Row::kBounded && !SIMD>(w, need4, count, q, &p);
         uint32_t f0 = 0, f1 = 0, fi = 0;
         float ferr = 0.0f;
         bool need3 = false;
@@ -1114,8 +1133,8 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         }
         __syncwarp();
         int my3;
-        if (NW > 1 && group) my3 = flat_search_group<false, NW>(*g, gsums, need3, count3, q);
-        else my3 = flat_search<false, SIMD>(w, need3, count3, q, &p);
+        if (NW > 1 && group) my3 = flat_search_group<false, NW, Row::kBounded>(*g, gsums, need3, count3, q);
+        else my3 = flat_search<false, SIMD, Row::kBounded && !SIMD>(w, need3, count3, q, &p);
         if (need3) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
             if (my3 >= 0) {
