@@ -552,7 +552,9 @@ __device__ __forceinline__ float fit_error(V3 a, V3 b, V3 ax, V3 bx, float alpha
 // One cluster_fit_four iteration (icbc.h:2650-2722), scalar arithmetic order.
 // BND (inputs of a kBounded row): e2 = t * 2 enters e1 only through
 // (b * b) * beta2 + e2, and t * 2 is exact when t cannot overflow, so the
-// product and that sum are one fused multiply-add with the same bits.
+// product and that sum are one fused multiply-add with the same bits; and
+// the determinant is +0 or of magnitude between 2^-100 and 2^100 (weights
+// are 0 or at least 1/255, sums at most 16), where rcp_bounded is 1 / d.
 template <bool BND = false>
 __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, const FitSums &k, const FitWeights &q,
                                           V3 &a, V3 &b) {
@@ -569,7 +571,7 @@ __device__ __forceinline__ float cf4_combo(const float *S, uint32_t packed, cons
     const float alpha2 = w2 * q.w1_9 + (w1 * q.w4_9 + w0);
     const float beta2 = w1 * q.w1_9 + (w2 * q.w4_9 + w3);
     const float ab = (w1 + w2) * q.w2_9;
-    const float factor = 1.0f / (alpha2 * beta2 - ab * ab);
+    const float factor = BND ? rcp_bounded(alpha2 * beta2 - ab * ab) : 1.0f / (alpha2 * beta2 - ab * ab);
     const V3 ax = v3(x2.x * q.w1_3 + (x1.x * q.w2_3 + x0.x), x2.y * q.w1_3 + (x1.y * q.w2_3 + x0.y),
                      x2.z * q.w1_3 + (x1.z * q.w2_3 + x0.z));
     const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
@@ -598,7 +600,7 @@ __device__ __forceinline__ float cf3_combo(const float *S, uint32_t packed, cons
     const float ab = w1 * 0.25f;
     const float alpha2 = w0 + ab;
     const float beta2 = w2 + ab;
-    const float factor = 1.0f / (alpha2 * beta2 - ab * ab);
+    const float factor = BND ? rcp_bounded(alpha2 * beta2 - ab * ab) : 1.0f / (alpha2 * beta2 - ab * ab);
     const V3 ax = BND ? v3(__fmaf_rn(x1.x, 0.5f, x0.x), __fmaf_rn(x1.y, 0.5f, x0.y), __fmaf_rn(x1.z, 0.5f, x0.z))
                       : x0 + x1 * 0.5f;
     const V3 bx = v3(k.r_sum - ax.x, k.g_sum - ax.y, k.b_sum - ax.z);
