@@ -925,6 +925,36 @@ __device__ __forceinline__ int flat_search(const WarpCtx &w, bool need, int coun
 // the CTA must call it together (it synchronises the CTA) with the same fit
 // weights `q`: every thread walks combinations of any of the group's blocks.
 // Same winner rule as flat_search: per block the smallest (error, table index).
+// Every walker of the group search runs exactly `per` steps: a walker that
+// passes the end of the list walks on into a sentinel block after the last
+// one (index 32 * NW: 16 colours, a SAT row of NaNs, set up by the kernel),
+// whose errors are NaN and never fold in, and a walker with no range starts
+// there.  So no step tests whether its walker is live.  The sentinel has 968
+// (or 152) combinations, more than a walker's `per` <= 484 (or 76) steps, so
+// no walker crosses out of it.
+template <bool FOUR, int NB>
+__device__ __forceinline__ void walker_start_s(const WarpCtx &w, Walker &v, int g, int W) {
+    int b = NB, k = 0;
+    if (g < W) {
+        int lo = 0, hi = NB;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if ((block_info(w, mid) & kInfoMask) <= g) lo = mid;
+            else hi = mid;
+        }
+        b = lo;
+        k = g - (block_info(w, lo) & kInfoMask);
+    }
+    walker_enter<FOUR>(w, v, b, k);
+}
+
+__device__ __forceinline__ void walker_fold_s(Walker &v, float e) {
+    const bool better = e < v.best;
+    v.best = better ? e : v.best;
+    v.best_k = better ? v.k : v.best_k;
+    v.k++;
+}
+
 template <bool FOUR, int NW, bool BND = false>
 __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bool need, int count,
                                                  const FitWeights &q) {
@@ -952,8 +982,8 @@ __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bo
     if (W == 0) return -1;
     const int per = (W + 64 * NW - 1) / (64 * NW);
     Walker A, B;
-    walker_start_n<FOUR, 32 * NW>(g, A, min(j * per, W), min(j * per + per, W));
-    walker_start_n<FOUR, 32 * NW>(g, B, min((j + 32 * NW) * per, W), min((j + 32 * NW) * per + per, W));
+    walker_start_s<FOUR, 32 * NW>(g, A, j * per, W);
+    walker_start_s<FOUR, 32 * NW>(g, B, (j + 32 * NW) * per, W);
     const uint32_t *table = FOUR ? g.T->four : g.T->three;
     uint32_t pa = table[A.k], pb = table[B.k];
     for (int it = 0; it < per; it++) {
@@ -961,9 +991,9 @@ __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bo
         V3 a, b;
         const float ea = FOUR ? cf4_combo<BND>(A.S, pa, A.sums, q, a, b) : cf3_combo<BND>(A.S, pa, A.sums, q, a, b);
         const float eb = FOUR ? cf4_combo<BND>(B.S, pb, B.sums, q, a, b) : cf3_combo<BND>(B.S, pb, B.sums, q, a, b);
-        walker_fold(A, ea);
-        walker_fold(B, eb);
-        const bool xa = walker_crossing(A), xb = walker_crossing(B);
+        walker_fold_s(A, ea);
+        walker_fold_s(B, eb);
+        const bool xa = A.k == A.total, xb = B.k == B.total;
         if (__any_sync(kFull, xa || xb)) {
             if (xa) walker_cross<FOUR>(g, A, na);
             if (xb) walker_cross<FOUR>(g, B, nb);

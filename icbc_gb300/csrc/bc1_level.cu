@@ -228,11 +228,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) k_image_listed(const Glo
 // output blocks.  All warps of an SM run the same stage's code at the same
 // time, and a search balances over 32 * NW blocks instead of 32.  Same
 // arithmetic and the same winner per block as k_image_listed.  Shared memory:
-// the tables, then the CTA's byte rows, SAT rows, argmin slots, info words
-// and NW scan sums (group_smem_bytes).
+// the tables, then the CTA's byte rows, SAT rows and the sentinel's SAT row,
+// argmin slots, info words with the sentinel's (padded to 16 bytes) and NW
+// scan sums (group_smem_bytes).
 template <int NW>
 __host__ __device__ constexpr size_t group_smem_bytes() {
-    return sizeof(SharedTables) + (size_t)NW * 32 * (kInWordsByte * 4 + kSatStride * 4 + 8 + 4) + NW * 4;
+    return sizeof(SharedTables) + (size_t)NW * 32 * (kInWordsByte * 4 + kSatStride * 4 + 8 + 4) + NW * 4 +
+           kSatStride * 4 + 16;
 }
 
 // The batched CTA-wide kernel's layout: the group layout (16-byte aligned
@@ -249,9 +251,14 @@ __device__ __forceinline__ void group_ctx(unsigned char *smem, const SharedTable
                                           WarpCtx &w, WarpCtx &g, int *&sums) {
     uint32_t *in = reinterpret_cast<uint32_t *>(smem + sizeof(SharedTables));
     float *sat = reinterpret_cast<float *>(in + NW * 32 * kInWordsByte);
-    unsigned long long *slots = reinterpret_cast<unsigned long long *>(sat + NW * 32 * kSatStride);
+    unsigned long long *slots = reinterpret_cast<unsigned long long *>(sat + (NW * 32 + 1) * kSatStride);
     int *info = reinterpret_cast<int *>(slots + NW * 32);
-    sums = info + NW * 32;
+    sums = info + NW * 32 + 4;
+    // The group search's sentinel block (flat_search_group), read only after
+    // the search's first barrier.
+    const float nan = __int_as_float(0x7fffffff);
+    if (threadIdx.x < 17) st4(sat + NW * 32 * kSatStride + 4 * threadIdx.x, make_float4(nan, nan, nan, nan));
+    if (threadIdx.x == 0) info[NW * 32] = 16 << kInfoShift;
     const int warp = threadIdx.x >> 5;
     g.T = &T;
     g.D = D;
