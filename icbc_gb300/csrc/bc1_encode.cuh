@@ -986,20 +986,25 @@ __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bo
     walker_start_s<FOUR, 32 * NW>(g, B, (j + 32 * NW) * per, W);
     const uint32_t *table = FOUR ? g.T->four : g.T->three;
     uint32_t pa = table[A.k], pb = table[B.k];
-    for (int it = 0; it < per; it++) {
-        uint32_t na = table[A.k + 1], nb = table[B.k + 1];
-        V3 a, b;
-        const float ea = FOUR ? cf4_combo<BND>(A.S, pa, A.sums, q, a, b) : cf3_combo<BND>(A.S, pa, A.sums, q, a, b);
-        const float eb = FOUR ? cf4_combo<BND>(B.S, pb, B.sums, q, a, b) : cf3_combo<BND>(B.S, pb, B.sums, q, a, b);
-        walker_fold_s(A, ea);
-        walker_fold_s(B, eb);
-        const bool xa = A.k == A.total, xb = B.k == B.total;
-        if (__any_sync(kFull, xa || xb)) {
-            if (xa) walker_cross<FOUR>(g, A, na);
-            if (xb) walker_cross<FOUR>(g, B, nb);
+    for (int it = 0; it < per;) {
+        // The warp runs, without crossing tests, as many steps as its first
+        // walker to reach the end of its block needs (at least one: a walker
+        // is never at its block's end here), then moves the walkers that
+        // reached it into their next block.
+        const int run = __reduce_min_sync(kFull, min(min(A.total - A.k, B.total - B.k), per - it));
+        for (int r = 0; r < run; r++) {
+            const uint32_t na = table[A.k + 1], nb = table[B.k + 1];
+            V3 a, b;
+            const float ea = FOUR ? cf4_combo<BND>(A.S, pa, A.sums, q, a, b) : cf3_combo<BND>(A.S, pa, A.sums, q, a, b);
+            const float eb = FOUR ? cf4_combo<BND>(B.S, pb, B.sums, q, a, b) : cf3_combo<BND>(B.S, pb, B.sums, q, a, b);
+            walker_fold_s(A, ea);
+            walker_fold_s(B, eb);
+            pa = na;
+            pb = nb;
         }
-        pa = na;
-        pb = nb;
+        it += run;
+        if (A.k == A.total) walker_cross<FOUR>(g, A, pa);
+        if (B.k == B.total) walker_cross<FOUR>(g, B, pb);
     }
     walker_flush(g, A);
     walker_flush(g, B);
