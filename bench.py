@@ -63,8 +63,8 @@ REDUCE_PER_BLOCK = 64      # reduce_colors per-texel tests (levels 2..9)
 # flushes between kernels, as a timed call runs.  Level 8's
 # figure includes ~46 MB of write-backs of the buffer that flushes L2 before
 # the step; level 9's is its own traffic (the image is read once, through L2).
-NCU_TRAFFIC_BYTES = {8: (67.18e6 + 49.04e6) + (18.72e6 + 11.34e6),
-                     9: (14.77e6 + 8.09e6) + (20.71e6 + 7.10e6) + (11.31e6 + 7.20e6)}
+NCU_TRAFFIC_BYTES = {8: (67.18e6 + 48.94e6) + (20.45e6 + 12.09e6),
+                     9: (15.97e6 + 9.10e6) + (21.56e6 + 7.68e6) + (11.61e6 + 7.52e6)}
 TRAFFIC_SOURCE = "one ncu capture of this workload with --cache-control none: dram__bytes_read.sum + " \
                  "dram__bytes_write.sum summed over the level call's launches"
 
@@ -77,10 +77,12 @@ def launches_per_level(level: int) -> int:
 
 
 def level_kernels(level: int) -> str:
-    """The launches of one level call on the RGBA8 image with alpha weights."""
+    """The launches of one level call on the RGBA8 image with alpha weights
+    (the default shapes: a CTA-wide listed pass from level 4 on)."""
     if level < 2:
         return "k_encode_image<%d>" % level
-    return "k_image_trivial<%d> + k_image_listed<%d>" % (level, level) + (" + k_refine<1>" if level == 9 else "")
+    listed = "k_image_listed<%d>" % level if level < 4 else "k_image_listed_cta<%d, %d, 16>" % (level, level == 9)
+    return "k_image_trivial<%d> + %s" % (level, listed) + (" + k_refine<1>" if level == 9 else "")
 
 
 def algorithmic_ops(stats: dict, level: int) -> float:
