@@ -955,7 +955,10 @@ __device__ __forceinline__ void walker_fold_s(Walker &v, float e) {
     v.k++;
 }
 
-template <bool FOUR, int NW, bool BND = false>
+// RUNS: step in runs between block crossings (levels 8-9, whose blocks have
+// hundreds of combinations); otherwise test for crossings after every step
+// (at levels 2-7 a warp's 64 walkers leave a block every step or two).
+template <bool FOUR, int NW, bool BND = false, bool RUNS = true>
 __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bool need, int count,
                                                  const FitWeights &q) {
     const int j = threadIdx.x;
@@ -991,7 +994,7 @@ __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bo
         // walker to reach the end of its block needs (at least one: a walker
         // is never at its block's end here), then moves the walkers that
         // reached it into their next block.
-        const int run = __reduce_min_sync(kFull, min(min(A.total - A.k, B.total - B.k), per - it));
+        const int run = RUNS ? __reduce_min_sync(kFull, min(min(A.total - A.k, B.total - B.k), per - it)) : 1;
         for (int r = 0; r < run; r++) {
             const uint32_t na = table[A.k + 1], nb = table[B.k + 1];
             V3 a, b;
@@ -1003,8 +1006,11 @@ __device__ __forceinline__ int flat_search_group(const WarpCtx &g, int *sums, bo
             pb = nb;
         }
         it += run;
-        if (A.k == A.total) walker_cross<FOUR>(g, A, pa);
-        if (B.k == B.total) walker_cross<FOUR>(g, B, pb);
+        const bool xa = A.k == A.total, xb = B.k == B.total;
+        if (RUNS || __any_sync(kFull, xa || xb)) {
+            if (xa) walker_cross<FOUR>(g, A, pa);
+            if (xb) walker_cross<FOUR>(g, B, pb);
+        }
     }
     walker_flush(g, A);
     walker_flush(g, B);
@@ -1136,7 +1142,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         // 4-colour cluster fit of every block that needs one, across the warp.
         const FitWeights q = fit_weights(w.D, metric);
         int my4;
-        if (NW > 1 && group) my4 = flat_search_group<true, NW, Row::kBounded>(*g, gsums, need4, count, q);
+        if (NW > 1 && group) my4 = flat_search_group<true, NW, Row::kBounded, (L >= 8)>(*g, gsums, need4, count, q);
         else my4 = flat_search<true, SIMD, Row::kBounded && !SIMD>(w, need4, count, q, &p);
         uint32_t f0 = 0, f1 = 0, fi = 0;
         float ferr = 0.0f;
@@ -1170,7 +1176,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
         }
         __syncwarp();
         int my3;
-        if (NW > 1 && group) my3 = flat_search_group<false, NW, Row::kBounded>(*g, gsums, need3, count3, q);
+        if (NW > 1 && group) my3 = flat_search_group<false, NW, Row::kBounded, (L >= 8)>(*g, gsums, need3, count3, q);
         else my3 = flat_search<false, SIMD, Row::kBounded && !SIMD>(w, need3, count3, q, &p);
         if (need3) {
             V3 a = v3(0.0f, 0.0f, 0.0f), b = a;
