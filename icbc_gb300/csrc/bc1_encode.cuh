@@ -142,11 +142,14 @@ __device__ __forceinline__ int reduce_colors(const Row &row, float threshold, fl
 //   stable insertion sort along the axis: replaced by stable ranks
 //     (position = #smaller + #equal-and-earlier), the same permutation for
 //     every non-NaN key; keys containing NaN take a literal insertion sort.
+// N: the unrolled width, 16 or, when count <= 8, 8 (the same sums in the
+// same order: the entries past count contribute nothing either way).
+template <int N = 16>
 __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool skip_black) {
-    float cx[16], cy[16], cz[16], cw[16];
+    float cx[N], cy[N], cz[N], cw[N];
     unsigned use = 0;
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < N; i++) {
         const bool in = i < count;
         const float4 c = ld4(srow + 4 * i);
         cx[i] = in ? c.x : 0.0f;
@@ -160,7 +163,7 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
     V3 centroid = v3(0.0f, 0.0f, 0.0f);
     float total = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < N; i++) {
         if (use & (1u << i)) {
             total += cw[i];
             centroid = centroid + v3(cx[i], cy[i], cz[i]) * cw[i];
@@ -169,7 +172,7 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
     centroid = centroid * (1.0f / total);
     float m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < N; i++) {
         if (use & (1u << i)) {
             const V3 a = v3(cx[i], cy[i], cz[i]) - centroid;
             const V3 b = a * cw[i];
@@ -192,10 +195,10 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
         }
         axis = v;
     }
-    float dps[16];
+    float dps[N];
     bool has_nan = false;
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
+    for (int i = 0; i < N; i++) {
         dps[i] = dot(v3(cx[i], cy[i], cz[i]), axis);
         has_nan |= ((use >> i) & 1) && (dps[i] != dps[i]);
     }
@@ -203,13 +206,13 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
     if (!has_nan) {
         // Stable ranks from the 120 pairs i < j: j sorts before i iff
         // dps[j] < dps[i]; otherwise i (the earlier one) sorts before j.
-        int pos[16];
+        int pos[N];
 #pragma unroll
-        for (int i = 0; i < 16; i++) pos[i] = 0;
+        for (int i = 0; i < N; i++) pos[i] = 0;
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
+        for (int i = 0; i < N; i++) {
 #pragma unroll
-            for (int j = i + 1; j < 16; j++) {
+            for (int j = i + 1; j < N; j++) {
                 const bool both = ((use >> i) & (use >> j) & 1) != 0;
                 const bool j_first = dps[j] < dps[i];
                 pos[i] += both && j_first;
@@ -217,26 +220,26 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
             }
         }
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
+        for (int i = 0; i < N; i++) {
             if (use & (1u << i)) st4(srow + 4 * (pos[i] + 1), make_float4(cx[i] * cw[i], cy[i] * cw[i], cz[i] * cw[i], cw[i]));
         }
     } else {
         // Literal stable insertion sort of the kept colours (NaN keys).  The
         // colours are copied to a local array first so that the dynamic
         // indexing here does not move the register arrays to local memory.
-        float lc[64];
+        float lc[4 * N];
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
+        for (int i = 0; i < N; i++) {
             lc[4 * i + 0] = cx[i];
             lc[4 * i + 1] = cy[i];
             lc[4 * i + 2] = cz[i];
             lc[4 * i + 3] = cw[i];
         }
-        int order[16];
-        float key[16];
+        int order[N];
+        float key[N];
         int k = 0;
 #pragma unroll
-        for (int i = 0; i < 16; i++)
+        for (int i = 0; i < N; i++)
             if (use & (1u << i)) { order[k] = i; key[k] = dps[i]; k++; }
         for (int i = 0; i < m; i++)
             for (int j = i; j > 0 && key[j] < key[j - 1]; j--) {
@@ -1110,8 +1113,12 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
     int count = 16;
     bool any_black = false, live = false, need4 = false;
 
+    if (active && O::cluster) count = reduce_colors(row, O::threshold, srow, any_black);
+    // Every lane's table fits 8 entries: the 8-wide SAT build (warp-uniform;
+    // levels 2-7, where most blocks reduce to a few colours: 2-4% faster at
+    // levels 2-4; at levels 8-9 the second build's code cost 0.4%).
+    const bool narrow = O::cluster && L <= 7 && !SIMD && __all_sync(kFull, !active || count <= 8);
     if (active) {
-        if (O::cluster) count = reduce_colors(row, O::threshold, srow, any_black);
         if (O::cluster && count <= 1) {
             err = trivial_block(w.D, w.T->lut255, row, p, xyz(ld4(srow)), count, c0, c1, idx);
         } else {
@@ -1129,7 +1136,8 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
                 }
             }
             if (O::cluster) {
-                build_sat_inplace(srow, count, false);
+                if (narrow) build_sat_inplace<8>(srow, count, false);
+                else build_sat_inplace(srow, count, false);
                 if (SIMD) fill_sat_tail(srow, count, p.simd_gather);
                 need4 = true;
             }
@@ -1166,7 +1174,7 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
                     // then build the table of the non-black ones.
                     bool ab;
                     reduce_colors(row, O::threshold, srow, ab);
-                    count3 = build_sat_inplace(srow, count, true);
+                    count3 = narrow ? build_sat_inplace<8>(srow, count, true) : build_sat_inplace(srow, count, true);
                     if (SIMD) fill_sat_tail(srow, count3, p.simd_gather);
                     need3 = count3 > 0;
                 } else {
