@@ -117,8 +117,13 @@ __device__ __forceinline__ int reduce_colors(const Row &row, float threshold, fl
                 if (near3(cj, ci, threshold)) {
                     const float wj = c4.w;
                     const float s = wj + wi;
-                    st4(rrow + 4 * j, make_float4((cj.x * wj + ci.x * wi) / s, (cj.y * wj + ci.y * wi) / s,
-                                                  (cj.z * wj + ci.z * wi) / s, s));
+                    if (Row::kBounded)
+                        st4(rrow + 4 * j, make_float4(div_bounded(cj.x * wj + ci.x * wi, s),
+                                                      div_bounded(cj.y * wj + ci.y * wi, s),
+                                                      div_bounded(cj.z * wj + ci.z * wi, s), s));
+                    else
+                        st4(rrow + 4 * j, make_float4((cj.x * wj + ci.x * wi) / s, (cj.y * wj + ci.y * wi) / s,
+                                                      (cj.z * wj + ci.z * wi) / s, s));
                     break;
                 }
             }
@@ -1057,7 +1062,11 @@ __device__ __forceinline__ bool reduce_to_one(const Row &row, float threshold, V
                 count = 1;
             } else if (near3(c, ct, threshold)) {
                 const float s = wc + wt;
-                c = v3((c.x * wc + ct.x * wt) / s, (c.y * wc + ct.y * wt) / s, (c.z * wc + ct.z * wt) / s);
+                if (Row::kBounded)
+                    c = v3(div_bounded(c.x * wc + ct.x * wt, s), div_bounded(c.y * wc + ct.y * wt, s),
+                           div_bounded(c.z * wc + ct.z * wt, s));
+                else
+                    c = v3((c.x * wc + ct.x * wt) / s, (c.y * wc + ct.y * wt) / s, (c.z * wc + ct.z * wt) / s);
                 wc = s;
             } else {
                 other = true;
