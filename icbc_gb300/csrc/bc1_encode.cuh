@@ -299,8 +299,10 @@ __device__ __forceinline__ bool optimize_end_points4(const Row &row, uint32_t in
 #pragma unroll 1
     for (int i = 0; i < 16; i++) {
         const uint32_t bits = indices >> (2 * i);
+        // beta = bits & 1, and for bits & 2 (1 + beta) / 3: the two possible
+        // quotients are the constants 1/3 and 2/3 as floats.
         float beta = (float)(bits & 1);
-        if (bits & 2) beta = (1 + beta) / 3.0f;
+        if (bits & 2) beta = (bits & 1) ? 2.0f / 3.0f : 1.0f / 3.0f;
         const float alpha = 1.0f - beta;
         alpha2 += alpha * alpha;
         beta2 += beta * beta;
