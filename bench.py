@@ -18,6 +18,7 @@ sample of the same workload.  Under torchrun each rank encodes its own replica
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -620,28 +621,48 @@ def serving_leg(ig, args, batched_gpix):
             y0, x0 = (k * 389) % (2049 - side), (k * 211) % (2049 - side)
             crops.append(np.ascontiguousarray(bases[k % 2][y0:y0 + side, x0:x0 + side]))
         pool[side] = crops
+    # Untimed warm-up: one request of every side and level through a server
+    # (first launches, callback and delivery threads, allocator state).
+    warm = ig.Server(40 << 30, max_inflight=args.serve_inflight, max_batch_images=1024)
+    wids = [warm.submit(pool[side][0], lv, ig.Decoder_D3D10,
+                        out=np.zeros((ig.blocks_of(side, side), 8), np.uint8))
+            for side in synth.SERVING_SIDES for lv in range(10)]
+    for rid in wids:
+        warm.wait(rid, 120000)
+    warm.close()
     runs = []
     for rate in args.serve_rates:
         n = int(min(args.serve_max_requests, max(400, rate * args.serve_seconds)))
         reqs = synth.serving_requests(n, rate, seed=int(rate))
+        # The callers' result buffers exist, touched, before the requests
+        # arrive (a client reuses its buffers): fresh pages would put the
+        # kernel's first-touch faults and zeroing on the delivery path.
         outs = [np.empty((ig.blocks_of(r.side, r.side), 8), np.uint8) for r in reqs]
+        for o in outs:
+            o.fill(0)
         srv = ig.Server(40 << 30, max_inflight=args.serve_inflight, max_batch_images=1024)
         ids = [None] * n
         nthreads = args.serve_threads
 
         def submitter(k, t0):
             # Thread k submits requests k, k + nthreads, ... at their arrival
-            # times (ctypes releases the GIL inside the call).
+            # times (ctypes releases the GIL inside the call).  Waits sleep
+            # (releasing the GIL) down to 50 us instead of spinning, so the
+            # submitting threads do not hold each other up by a switch interval.
             for i in range(k, n, nthreads):
                 r = reqs[i]
                 while True:
                     dt = r.arrival_s - (time.perf_counter() - t0)
                     if dt <= 0:
                         break
-                    if dt > 2e-3:
-                        time.sleep(dt - 1e-3)
+                    if dt > 5e-5:
+                        time.sleep(dt * 0.8)
                 ids[i] = srv.submit(pool[r.side][i % 3], r.level, ig.Decoder_D3D10, out=outs[i])
 
+        # No garbage-collector pause inside the timed run: one would hold the
+        # submitting threads and release their requests in a burst.
+        gc.collect()
+        gc.disable()
         t0 = time.perf_counter()
         threads = [threading.Thread(target=submitter, args=(k, t0)) for k in range(nthreads)]
         for t in threads:
@@ -652,6 +673,7 @@ def serving_leg(ig, args, batched_gpix):
         for rid in ids:
             srv.wait(rid, 120000)
         wall = time.perf_counter() - t0
+        gc.enable()
         st = srv.stats()
         srv.close()
         px = sum(r.side * r.side for r in reqs)

@@ -81,16 +81,25 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 6)
     }
 }
 
-cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
-                                 const uint32_t *task_start, int n_images, int ntasks, BatchLists lists,
-                                 const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream, int sms) {
-    if (ntasks <= 0) return cudaSuccess;
+// CTAs of k_batch_trivial per SM; the query also loads the kernel's code
+// (modules load on first use), so a caller can take that cost up front.
+static int batch_trivial_resident() {
     static int resident = 0;
     if (!resident &&
         (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_batch_trivial, kWarpsPerCta * 32, 0) !=
              cudaSuccess ||
          resident < 1))
         resident = 1;
+    return resident;
+}
+
+void prepare_batch_trivial() { batch_trivial_resident(); }
+
+cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
+                                 const uint32_t *task_start, int n_images, int ntasks, BatchLists lists,
+                                 const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream, int sms) {
+    if (ntasks <= 0) return cudaSuccess;
+    const int resident = batch_trivial_resident();
     const int64_t need = ((int64_t)ntasks + kWarpsPerCta - 1) / kWarpsPerCta;
     const int64_t cap = (int64_t)sms * resident;
     const int grid = (int)(need < cap ? need : cap);

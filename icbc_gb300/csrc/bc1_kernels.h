@@ -125,6 +125,8 @@ inline cudaError_t launch_encode_batch(const GlobalTables *G, const ImageDesc *i
 cudaError_t launch_batch_trivial(const GlobalTables *G, const ImageDesc *images, const BatchTask *tasks,
                                  const uint32_t *task_start, int n_images, int ntasks, BatchLists lists,
                                  const int64_t *refine_base, RefineSlot *slots, cudaStream_t stream, int sms);
+// Loads launch_batch_trivial's kernel (which otherwise loads on its first launch).
+void prepare_batch_trivial();
 inline int batch_ctas_per_sm(bool byte_rows = false) {
     return byte_rows ? batch_ctas_per_sm_bytes() : batch_ctas_per_sm_float();
 }

@@ -390,7 +390,10 @@ int icbc_gpu_server_create(const icbc_gpu_server_config *config, icbc_gpu_server
     cudaGetDevice(&S->device);
     int per_sm = 1;
     cudaDeviceGetAttribute(&S->grid, cudaDevAttrMultiProcessorCount, S->device);
+    // Both queries load the server's kernels now (modules load on first
+    // use), not inside the first launches.
     per_sm = batch_ctas_per_sm(true);
+    prepare_batch_trivial();
     S->grid *= per_sm;
     const size_t budget = round_up((size_t)config->hbm_budget_bytes, kGranule);
     // Pinned staging for blocks and errors (an eighth and a sixteenth of the
