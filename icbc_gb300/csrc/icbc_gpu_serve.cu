@@ -15,6 +15,9 @@
 // A launch runs in the batched form's two passes: the blocks of 0 or 1
 // reduced colours of level-2..9 requests are finished by a register-only
 // pass, which lists the others in the request's own arena space.
+// Light requests (under ~0.2 ms of GPU time) and heavy ones go to separate
+// launches, light first: a launch completes as a whole, so a small request
+// batched with a large one would wait for it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -103,6 +106,7 @@ struct Request {
     size_t in_off = 0, in_bytes = 0;  // pinned copy of the texels (rows at dpitch), then at levels 4-9 the
                                       // zero blocks the encoder starts from, laid out as on the device
     bool staged = false;
+    bool heavy = false;  // about 0.2 ms of GPU time or more (heavy_request)
     double t_submit = 0.0;
 };
 
@@ -143,6 +147,7 @@ struct icbc_gpu_server {
     std::mutex m;
     std::condition_variable cv_work, cv_done;
     std::deque<Request *> pending, admitted;
+    bool heavy_turn = false;  // light and heavy launches alternate while both wait
     // Finished launches (requests, status) waiting for their host copies.
     std::deque<std::pair<std::vector<Request *>, int>> delivery;
     std::condition_variable cv_deliver;
@@ -161,6 +166,14 @@ struct icbc_gpu_server {
 };
 
 namespace {
+
+// Whether a request alone takes about 0.2 ms of GPU time or more: blocks
+// times the encoder's nanoseconds per block at its level on a GB300 (the
+// quality-sweep image, a whole GPU).
+bool heavy_request(const ImageDesc &d) {
+    static const double kBlockNs[10] = {0.09, 0.15, 0.11, 0.12, 0.19, 0.38, 0.65, 1.0, 3.7, 4.5};
+    return (double)d.nblocks * kBlockNs[d.level < 0 ? 0 : d.level > 9 ? 9 : d.level] >= 2.0e5;
+}
 
 // Device and pinned bytes a request needs.
 void size_request(icbc_gpu_server *S, Request *q) {
@@ -349,14 +362,28 @@ void scheduler(icbc_gpu_server *S) {
             S->admitted.push_back(q);
             S->arena_peak = std::max<int64_t>(S->arena_peak, (int64_t)S->dev.used());
         }
-        // Launch everything admitted on a free slot.
+        // Launch the admitted requests on a free slot: the light ones
+        // together or the heavy ones together -- the light ones when only
+        // they wait, and when both wait, light and heavy in turn (so heavy
+        // requests are not held back for good under a stream of light ones).
         Slot *free_slot = nullptr;
         for (Slot &slot : S->slots)
             if (!slot.busy) { free_slot = &slot; break; }
         if (free_slot && !S->admitted.empty()) {
-            const size_t n = std::min<size_t>(S->admitted.size(), (size_t)S->cfg.max_batch_images);
-            free_slot->reqs.assign(S->admitted.begin(), S->admitted.begin() + n);
-            S->admitted.erase(S->admitted.begin(), S->admitted.begin() + n);
+            const bool any_light =
+                std::any_of(S->admitted.begin(), S->admitted.end(), [](const Request *q) { return !q->heavy; });
+            const bool any_heavy =
+                std::any_of(S->admitted.begin(), S->admitted.end(), [](const Request *q) { return q->heavy; });
+            const bool light = any_light && !(any_heavy && S->heavy_turn);
+            if (any_light && any_heavy) S->heavy_turn = !S->heavy_turn;
+            std::vector<Request *> &take = free_slot->reqs;
+            take.clear();
+            std::deque<Request *> rest;
+            for (Request *q : S->admitted) {
+                if (q->heavy != light && take.size() < (size_t)S->cfg.max_batch_images) take.push_back(q);
+                else rest.push_back(q);
+            }
+            S->admitted.swap(rest);
             free_slot->busy = true;
             S->in_flight++;
             S->batches++;
@@ -462,6 +489,7 @@ int icbc_gpu_server_submit(icbc_gpu_server *S, const icbc_gpu_request *req, uint
         return st;
     }
     size_request(S, q);
+    q->heavy = heavy_request(q->d);
     const size_t img = round_up((size_t)q->dpitch * req->height, kGranule);
     q->out_off = img;
     q->err_off = img + round_up((size_t)q->d.nblocks * 8, kGranule);
