@@ -147,8 +147,8 @@ __device__ __forceinline__ int reduce_colors(const Row &row, float threshold, fl
 //   stable insertion sort along the axis: replaced by stable ranks
 //     (position = #smaller + #equal-and-earlier), the same permutation for
 //     every non-NaN key; keys containing NaN take a literal insertion sort.
-// N: the unrolled width, 16 or, when count <= 8, 8 (the same sums in the
-// same order: the entries past count contribute nothing either way).
+// N: the unrolled width, 16 or, when count <= N, 8 or 12 (the same sums in
+// the same order: the entries past count contribute nothing either way).
 template <int N = 16>
 __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool skip_black) {
     float cx[N], cy[N], cz[N], cw[N];
@@ -1125,10 +1125,12 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
     bool any_black = false, live = false, need4 = false;
 
     if (active && O::cluster) count = reduce_colors(row, O::threshold, srow, any_black);
-    // Every lane's table fits 8 entries: the 8-wide SAT build (warp-uniform;
-    // levels 2-7, where most blocks reduce to a few colours: 2-4% faster at
-    // levels 2-4; at levels 8-9 the second build's code cost 0.4%).
-    const bool narrow = O::cluster && L <= 7 && !SIMD && __all_sync(kFull, !active || count <= 8);
+    // The SAT build unrolled no wider than the warp's largest colour count
+    // needs: 8, 12 or 16 entries (warp-uniform; levels 2-7, where most
+    // blocks reduce to a few colours; at levels 8-9 the extra builds' code
+    // cost 0.4%).
+    const int wmax = O::cluster && L <= 7 && !SIMD ? __reduce_max_sync(kFull, active ? count : 0) : 16;
+    const int width = wmax <= 8 ? 8 : wmax <= 12 ? 12 : 16;
     if (active) {
         if (O::cluster && count <= 1) {
             err = trivial_block(w.D, w.T->lut255, row, p, xyz(ld4(srow)), count, c0, c1, idx);
@@ -1147,7 +1149,8 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
                 }
             }
             if (O::cluster) {
-                if (narrow) build_sat_inplace<8>(srow, count, false);
+                if (width == 8) build_sat_inplace<8>(srow, count, false);
+                else if (width == 12) build_sat_inplace<12>(srow, count, false);
                 else build_sat_inplace(srow, count, false);
                 if (SIMD) fill_sat_tail(srow, count, p.simd_gather);
                 need4 = true;
@@ -1185,7 +1188,9 @@ __device__ __forceinline__ float encode_warp_ex(const WarpCtx &w, const Row &row
                     // then build the table of the non-black ones.
                     bool ab;
                     reduce_colors(row, O::threshold, srow, ab);
-                    count3 = narrow ? build_sat_inplace<8>(srow, count, true) : build_sat_inplace(srow, count, true);
+                    count3 = width == 8    ? build_sat_inplace<8>(srow, count, true)
+                             : width == 12 ? build_sat_inplace<12>(srow, count, true)
+                                           : build_sat_inplace(srow, count, true);
                     if (SIMD) fill_sat_tail(srow, count3, p.simd_gather);
                     need3 = count3 > 0;
                 } else {
