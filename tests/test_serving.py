@@ -59,6 +59,30 @@ def test_alone_equals_mix_equals_plain(gpu_lib):
         srv.close()
 
 
+def test_heavy_and_light_requests(gpu_lib):
+    """Heavy requests (1024^2 at levels 7-9: over 0.2 ms of GPU time each,
+    and more tasks than the GPU has CTA slots, so their launches take three
+    quarters of the slots) and light ones submitted together: they go to
+    separate launches, light first and in turn, and every result equals the
+    plain encode."""
+    big = synth.gradient_noise_rects(1024, 1024, 17)
+    heavy = [(np.ascontiguousarray(np.roll(big, 64 * k, axis=1)), 7 + k % 3, k % 3) for k in range(4)]
+    light = _requests(30, 5)
+    order = light[:10] + heavy[:2] + light[10:20] + heavy[2:] + light[20:]
+    srv = ig.Server(1 << 30, max_inflight=8, max_batch_images=64)
+    try:
+        ids = [srv.submit(img, lv, dec) for img, lv, dec in order]
+        for rid in ids:
+            assert srv.wait(rid, 60000) == 0
+        for (img, lv, dec), rid in zip(order, ids):
+            assert np.array_equal(srv.result(rid)[0], _plain(img, lv, dec)), (img.shape, lv, dec)
+        st = srv.stats()
+        assert st["completed"] == len(order) and st["failed"] == 0
+        assert st["batches"] >= 2  # the heavy ones never share the light ones' launch
+    finally:
+        srv.close()
+
+
 def test_two_pass_edge_requests(gpu_lib):
     """Launches finish the blocks of 0 or 1 reduced colours of level-2..9
     requests first and list the rest: flat requests (empty lists), noise
