@@ -630,8 +630,7 @@ def serving_leg(ig, args, batched_gpix):
     for rid in wids:
         warm.wait(rid, 120000)
     warm.close()
-    runs = []
-    for rate in args.serve_rates:
+    def run_once(rate):
         n = int(min(args.serve_max_requests, max(400, rate * args.serve_seconds)))
         reqs = synth.serving_requests(n, rate, seed=int(rate))
         # The callers' result buffers exist, touched, before the requests
@@ -677,11 +676,23 @@ def serving_leg(ig, args, batched_gpix):
         st = srv.stats()
         srv.close()
         px = sum(r.side * r.side for r in reqs)
-        runs.append({"rate_req_s": rate, "requests": n, "offered_gpix_s": px / reqs[-1].arrival_s / 1e9,
-                     "achieved_submit_rate_req_s": n / submit_span, "submit_threads": nthreads,
-                     "gpix_s": st["pixels_completed"] / wall / 1e9, "p50_ms": st["latency_p50_ms"],
-                     "p99_ms": st["latency_p99_ms"], "mean_ms": st["latency_mean_ms"], "max_ms": st["latency_max_ms"],
-                     "batches": st["batches"], "arena_peak_bytes": st["arena_peak"], "completed": st["completed"]})
+        return {"rate_req_s": rate, "requests": n, "offered_gpix_s": px / reqs[-1].arrival_s / 1e9,
+                "achieved_submit_rate_req_s": n / submit_span, "submit_threads": nthreads,
+                "gpix_s": st["pixels_completed"] / wall / 1e9, "p50_ms": st["latency_p50_ms"],
+                "p99_ms": st["latency_p99_ms"], "mean_ms": st["latency_mean_ms"], "max_ms": st["latency_max_ms"],
+                "batches": st["batches"], "arena_peak_bytes": st["arena_peak"], "completed": st["completed"]}
+
+    # Each rate runs serve_repeats times (a fresh server each time); the
+    # line reports the run with the median p99 and lists every run's
+    # Gpixel/s, p50 and p99 (the host is shared, so a run can catch a stall
+    # of the machine's other work).
+    runs = []
+    for rate in args.serve_rates:
+        reps = [run_once(rate) for _ in range(max(1, args.serve_repeats))]
+        med = sorted(reps, key=lambda r: r["p99_ms"])[(len(reps) - 1) // 2]
+        med = dict(med, repeats=len(reps), gpix_s_all=[r["gpix_s"] for r in reps],
+                   p50_ms_all=[r["p50_ms"] for r in reps], p99_ms_all=[r["p99_ms"] for r in reps])
+        runs.append(med)
     return {"workload": "poisson_serving", "hbm_budget_bytes": 40 << 30, "max_inflight": args.serve_inflight,
             "batched_offline_gpix_s": batched_gpix, "runs": runs,
             "saturation": {"rate_req_s": runs[-1]["rate_req_s"], "gpix_s": runs[-1]["gpix_s"],
@@ -809,6 +820,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--serve-max-requests", type=int, default=8000)
     ap.add_argument("--serve-threads", type=int, default=4)
+    ap.add_argument("--serve-repeats", type=int, default=3,
+                    help="runs per serving rate; the line reports the median-p99 run and lists all")
     ap.add_argument("--serve-inflight", type=int, default=8, help="batched launches the server keeps on the GPU")
     args = ap.parse_args()
     if args.levels:
