@@ -512,13 +512,27 @@ int icbc_gpu_batch_create(const icbc_gpu_image *images, int n_images, icbc_gpu_b
     const GlobalTables *G = nullptr;
     int st = ensure_device_tables(&G);
     if (st) return st;
-    // Tasks of 32 blocks, most expensive level first, larger images first
-    // inside a level, so the tail of the persistent launch is cheap work.
+    // Tasks of 32 blocks, most expensive level first; inside a level the
+    // images with the same decoder and colour weights together (the CTA-wide
+    // kernels search a round's blocks together only when its tasks share
+    // them), larger images first, so the tail of each launch is cheap work.
     std::vector<int> order((size_t)n_images);
     for (int i = 0; i < n_images; i++) order[i] = i;
+    auto cw_key = [&](int i) {
+        uint64_t k = 0;
+        for (int c = 0; c < 3; c++) {
+            uint32_t u;
+            std::memcpy(&u, &descs[i].cw[c], 4);
+            k = k * 0x9e3779b97f4a7c15ull + u;
+        }
+        return k;
+    };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         if (kLevelCost[descs[a].level] != kLevelCost[descs[b].level])
             return kLevelCost[descs[a].level] > kLevelCost[descs[b].level];
+        if (descs[a].decoder != descs[b].decoder) return descs[a].decoder < descs[b].decoder;
+        const uint64_t ka = cw_key(a), kb = cw_key(b);
+        if (ka != kb) return ka < kb;
         return descs[a].nblocks > descs[b].nblocks;
     });
     std::vector<int> own;  // images that get their level's own launch
