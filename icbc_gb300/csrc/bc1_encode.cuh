@@ -209,8 +209,9 @@ __device__ __forceinline__ int build_sat_inplace(float *srow, int count, bool sk
     }
     st4(srow, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     if (!has_nan) {
-        // Stable ranks from the 120 pairs i < j: j sorts before i iff
-        // dps[j] < dps[i]; otherwise i (the earlier one) sorts before j.
+        // Stable ranks from the pairs i < j (120 at width 16): j sorts
+        // before i iff dps[j] < dps[i]; otherwise i (the earlier one) sorts
+        // before j.
         int pos[N];
 #pragma unroll
         for (int i = 0; i < N; i++) pos[i] = 0;
