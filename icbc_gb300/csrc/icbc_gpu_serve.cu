@@ -16,8 +16,10 @@
 // reduced colours of level-2..9 requests are finished by a register-only
 // pass, which lists the others in the request's own arena space.
 // Light requests (under ~0.2 ms of GPU time) and heavy ones go to separate
-// launches, light first: a launch completes as a whole, so a small request
-// batched with a large one would wait for it.
+// launches -- light first, the two in turn while both wait -- because a
+// launch completes as a whole, so a small request batched with a large one
+// would wait for it; and a launch with more tasks than the GPU has CTA slots
+// takes three quarters of them, so launches behind it start on the rest.
 #include <cuda_runtime.h>
 
 #include <algorithm>
