@@ -289,7 +289,7 @@ def run_reference(args):
     step_times = []
     per_level = {lv: [] for lv in LEVELS}
     for _ in range(args.steps):
-        times, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS, form=args.cpu_form)
+        times, _, outs = cpu_sweep(sample, nthreads, levels=LEVELS, form=args.cpu_form)
         step_times.append(sum(times.values()))
         for lv in LEVELS:
             per_level[lv].append(times[lv])
@@ -297,7 +297,10 @@ def run_reference(args):
     value = len(LEVELS) * px / t / 1e9
     # The other form, one untimed-by-the-contract sweep, for comparison.
     other = "scalar" if args.cpu_form != "scalar" else "neon-vector"
-    otimes, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS, form=other)
+    otimes, _, oouts = cpu_sweep(sample, nthreads, levels=LEVELS, form=other)
+    # Blocks where the NEON form's output differs from the scalar build's.
+    neon_outs, scalar_outs = (outs, oouts) if args.cpu_form != "scalar" else (oouts, outs)
+    neon_diff = {str(lv): int((neon_outs[lv] != scalar_outs[lv]).any(1).sum()) for lv in LEVELS}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
@@ -306,8 +309,12 @@ def run_reference(args):
         "per_level": {str(lv): len(per_level[lv]) and px / statistics.mean(per_level[lv]) / 1e9 for lv in LEVELS},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": sample_text(args.cpu_stride, px), "build": CPU_FORMS[args.cpu_form]["build"],
+                         "ms_per_step_mean_min": [t * 1e3, min(step_times) * 1e3],
                          other: {"value": len(LEVELS) * px / sum(otimes.values()) / 1e9,
-                                 "build": CPU_FORMS[other]["build"]}},
+                                 "build": CPU_FORMS[other]["build"]},
+                         "neon_blocks_differing_from_scalar": {"total": sum(neon_diff.values()),
+                                                               "blocks_per_level": len(outs[LEVELS[0]]),
+                                                               "per_level": neon_diff}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -418,7 +425,8 @@ def run_ours(args):
     nthreads = os.cpu_count() or 1
     ctimes, cstats, couts = cpu_sweep(sample, nthreads, levels=LEVELS)
     cpu_scalar = len(LEVELS) * sample_px / sum(ctimes.values()) / 1e9
-    vtimes, _, _ = cpu_sweep(sample, nthreads, levels=LEVELS, form="neon-vector")
+    vtimes, _, vouts = cpu_sweep(sample, nthreads, levels=LEVELS, form="neon-vector")
+    neon_diff = {str(lv): int((vouts[lv] != couts[lv]).any(1).sum()) for lv in LEVELS}
     cpu_value = len(LEVELS) * sample_px / sum(vtimes.values()) / 1e9
     bw = w // 4
     rows = list(range(0, h // 4, args.cpu_stride))
@@ -465,7 +473,10 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": sample_text(args.cpu_stride, sample_px),
                          "build": CPU_FORMS["neon-vector"]["build"],
-                         "scalar": {"value": cpu_scalar, "build": CPU_FORMS["scalar"]["build"]}},
+                         "scalar": {"value": cpu_scalar, "build": CPU_FORMS["scalar"]["build"]},
+                         "neon_blocks_differing_from_scalar": {"total": sum(neon_diff.values()),
+                                                               "blocks_per_level": int(couts[LEVELS[0]].shape[0]),
+                                                               "per_level": neon_diff}},
         "e2e": {"value": e2e["value"] if e2e else None, "unit": UNIT,
                 "h2d_bytes_per_step": e2e["h2d"] if e2e else None, "d2h_bytes_per_step": e2e["d2h"] if e2e else None,
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step",
