@@ -480,7 +480,8 @@ def run_ours(args):
         "e2e": {"value": e2e["value"] if e2e else None, "unit": UNIT,
                 "h2d_bytes_per_step": e2e["h2d"] if e2e else None, "d2h_bytes_per_step": e2e["d2h"] if e2e else None,
                 "path": "icbc_gpu_compress_bc1_image_host, pinned host buffers, 10 calls per step",
-                "steps": e2e["steps"] if e2e else None, "ms_per_step_min_max": e2e["min_max"] if e2e else None},
+                "steps": e2e["steps"] if e2e else None, "ms_per_step_min_max": e2e["min_max"] if e2e else None,
+                "per_level_ms": e2e["per_level_ms"] if e2e else None},
         "autotune": tuning,
         "batch": batch,
         "serving": serving,
@@ -503,10 +504,13 @@ def e2e_leg(ig, torch, img, nb, px, ws, args):
         ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
     steps = max(3, args.steps)
     times = []
+    per_level = {lv: [] for lv in LEVELS}
     for _ in range(steps):
         t0 = time.perf_counter()
         for lv in LEVELS:
+            tl = time.perf_counter()
             ig.compress_image_host(host_img, lv, ig.Decoder_D3D10, CW, ig.WEIGHTS_ALPHA, out=host_out[lv])
+            per_level[lv].append(time.perf_counter() - tl)
         times.append(time.perf_counter() - t0)
     t = statistics.mean(times)
     if ws > 1:  # the job's time is its slowest rank's
@@ -514,7 +518,8 @@ def e2e_leg(ig, torch, img, nb, px, ws, args):
     h2d = len(LEVELS) * img.nbytes + sum(nb * 8 for lv in LEVELS if lv >= 4)
     d2h = len(LEVELS) * nb * 8
     return {"value": ws * len(LEVELS) * px / t / 1e9, "h2d": h2d, "d2h": d2h, "steps": steps,
-            "min_max": [min(times) * 1e3, max(times) * 1e3]}
+            "min_max": [min(times) * 1e3, max(times) * 1e3],
+            "per_level_ms": {str(lv): statistics.mean(per_level[lv]) * 1e3 for lv in LEVELS}}
 
 
 def batch_leg(ig, torch, dev, args):

@@ -870,13 +870,16 @@ int icbc_gpu_compress_bc1_image_host(const uint8_t *rgba, int32_t width, int32_t
     if (e == cudaSuccess && weight_mode == ICBC_GPU_WEIGHTS_PLANE)
         e = grow(reinterpret_cast<void **>(&H.d_plane), &H.plane_bytes, sizeof(float) * (size_t)width * height);
     if (e != cudaSuccess) return set_cuda_error(e);
-    // Bands of at least 64 block rows (whole block rows, so each band is an
-    // independent image whose last band alone meets the bottom edge).  Level
-    // 9 takes at most two bands of 256+ block rows: its refinement queue
-    // needs many blocks per lane to balance (in eight bands it was 8% slower
-    // end to end, in two 3% faster; every other level gains 5-40% from eight).
-    const int bands = level == 9 ? (int)std::max<int64_t>(1, std::min<int64_t>(2, bh / 256))
-                                 : (int)std::max<int64_t>(1, std::min<int64_t>(kMaxBands, bh / 64));
+    // Bands of whole block rows (each band is an independent image whose
+    // last band alone meets the bottom edge), at most kLevelBands[level] of
+    // at least 512 / that many block rows each.  The light levels take eight
+    // (their upload is most of the call, and eight bands overlap it with the
+    // encode); levels 6-7 four and 8-9 two: a band of an eighth of the image
+    // is too small for the listed pass's 16-warp CTAs and leaves a tail per
+    // band, and level 9's refinement queue needs many blocks per lane.
+    static const int kLevelBands[10] = {8, 8, 8, 8, 8, 8, 4, 4, 2, 2};
+    const int cap_bands = std::min(kMaxBands, kLevelBands[level < 0 ? 0 : level > 9 ? 9 : level]);
+    const int bands = (int)std::max<int64_t>(1, std::min<int64_t>(cap_bands, bh / (512 / cap_bands)));
     const int64_t rows_per = (bh + bands - 1) / bands;
     int st = ICBC_GPU_OK;
     for (int i = 0; i < bands && st == ICBC_GPU_OK; i++) {
