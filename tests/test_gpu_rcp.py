@@ -3,8 +3,9 @@ div_bounded in icbc_gb300/csrc/bc1_device.cuh) against the IEEE division.
 rcp_bounded equals 1.0f / d for every float d with 2^-100 <= |d| <= 2^100
 and for +-0, the range its callers can reach (all 3.4e9 values);
 div_bounded equals a / b for every float b in [2^-9, 64] with 16 dividends
-a in [0, 64] each (2e9 pairs).  The check program is compiled here with the
-encoder's flags."""
+each -- 0, seven spread over the floats of [2^-24, 64], eight uniform in
+[0, 64) -- its domain (2e9 pairs).  The check program is compiled here with
+the encoder's flags."""
 import os
 import struct
 import subprocess
